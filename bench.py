@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Swarm log-likelihood evaluations/s on the glycine-like workload
+(N=4000 training points, d=24 features, rbf ARD over 17 dims + periodic over
+7 dihedrals, concentrated likelihood, swarm of 40 particles) -- one "step" is
+one PSO iteration's swarm evaluated in one graph-captured batched pass.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fgpu|reference]
+
+* value       : swarm evaluations/s with theta already resident in HBM
+                (device-pointer entry point), max time over ranks.
+* e2e         : the same metric through the public batched C-ABI call with
+                host buffers (theta H2D and ll/info D2H inside the timed region).
+* plain       : evaluations/s of the one-particle-per-call drop-in.
+* roofline    : the dominant kernel's (trailing update, FP64 MMA) achieved
+                FP64 rate over its CUDA-event time inside the timed region,
+                against FP64 peak measured live (cuBLAS DGEMM).
+* cpu_baseline: the C restatement of the reference's OpenMP CPU path on a
+                bounded sample of particles, all host cores.
+Inputs are larger than L2: each step writes 40 K matrices (5.3 GB).
+``--impl reference`` times only the CPU restatement (the reference itself is
+Fortran and cannot be built on these machines).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "ferebus-v7_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "swarm logL evals/s (N=4000,d=24) batched vs plain on 1 GB300; FP64/HBM roofline %"
+UNIT = "evals/s"
+WORKLOAD = "glycine-like swarm: N=4000, d=24 (rbf 17 dims + periodic 7 dihedrals), concentrated, S=40"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def update_flops(N, nrhs, tb=64):
+    """Algorithmic flops of all trailing updates of one factorisation:
+    step s updates the lower triangle (incl. diagonal) of the remaining
+    t = N - tb (s+1) columns plus the nrhs right-hand-side rows, rank tb."""
+    tot = 0.0
+    s = 0
+    while True:
+        t = N - tb * (s + 1)
+        if t <= 0:
+            break
+        tot += 2.0 * tb * (t * (t + 1) / 2.0 + nrhs * t)
+        s += 1
+    return tot
+
+
+def fp64_peak_tflops(torch):
+    """Live FP64 peak: cuBLAS DGEMM 8192^3, best of 3."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def cpu_baseline(problem, mu, sample, threads):
+    """Time the C restatement of the reference's CPU path on ``sample`` particles."""
+    from oracle.build_ref import RefCPU
+    ref = RefCPU(problem.X, problem.y, mu, problem.kspec, problem.likelihood, problem.noise,
+                 problem.optimise_noise)
+    th = problem.thetas(sample, seed=7)
+    t0 = time.perf_counter()
+    ll, info = ref.loglik_batch(th, threads)
+    dt = time.perf_counter() - t0
+    ref.close()
+    return sample / dt, dt, ll, info
+
+
+def host_info():
+    try:
+        model = subprocess.run("lscpu | grep 'Model name' | head -1", shell=True, capture_output=True,
+                               text=True).stdout.split(":")[-1].strip()
+    except Exception:
+        model = "unknown"
+    return os.cpu_count(), model
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        if rank != 0:
+            dist.barrier()
+            dist.destroy_process_group()
+            return
+    from fgpu import synth
+    from fgpu.gpr import mean_vector
+    p = synth.config3()
+    mu = mean_vector(p.mean, p.X, p.y)
+    cores, model = host_info()
+    sample = args.ref_sample or cores
+    from oracle.build_ref import RefCPU
+    ref = RefCPU(p.X, p.y, mu, p.kspec, p.likelihood, p.noise, p.optimise_noise)
+    th = p.thetas(sample * (args.warmup + args.steps), seed=11)
+    for w in range(args.warmup):
+        ref.loglik_batch(th[w * sample:(w + 1) * sample], cores)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        o = (args.warmup + k) * sample
+        ref.loglik_batch(th[o:o + sample], cores)
+    dt = (time.perf_counter() - t0) / args.steps
+    ref.close()
+    v = sample / dt
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, shapes of the glycine-like config)",
+            "config": {"workload": WORKLOAD, "N": p.N, "d": p.d, "swarm_sample_per_step": sample},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{sample} particles per step ({model}); C restatement of the "
+                                       "reference's OpenMP path (distance tensors + dgemv + dpotrf/dpotrs)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fgpu", choices=("fgpu", "reference"))
+    ap.add_argument("--swarm", type=int, default=40)
+    ap.add_argument("--plain", type=int, default=4, help="particles timed on the plain path")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="particles in the CPU baseline sample")
+    ap.add_argument("--ref-sample", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from fgpu import Engine, Plan, synth
+    from fgpu.build import build_library
+    from fgpu.gpr import mean_vector
+    build_library()
+
+    p = synth.config3()
+    mu = mean_vector(p.mean, p.X, p.y)
+    eng = Engine(p.X, p.y, mu, p.kspec, p.likelihood, p.noise, p.optimise_noise)
+    S = args.swarm
+    plan = Plan([eng] * S)
+    nth = eng.ntheta
+    total = args.warmup + args.steps
+    th_host = p.thetas(S * total, seed=1 + rank).reshape(total, S, nth)
+    th_dev = torch.tensor(th_host, dtype=torch.float64, device="cuda")
+    ll_dev = torch.empty((total, S), dtype=torch.float64, device="cuda")
+    info_dev = torch.empty((total, S), dtype=torch.int32, device="cuda")
+    # a dedicated stream: the plan's graph, the timing events and the
+    # synchronisation below all live on it (torch's default stream has handle 0,
+    # which the C-ABI would read as "use the plan's own stream")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    plan.set_profiling(True)
+
+    def step(k):
+        plan.run_device(th_dev[k].data_ptr(), ll_dev[k].data_ptr(), info_dev[k].data_ptr(), stream.cuda_stream)
+
+    for w in range(args.warmup):
+        step(w)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(args.steps):
+            step(args.warmup + k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches_per_step = plan.launches()
+    ms = e0.elapsed_time(e1) / args.steps
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t)
+    value = S * ws / (ms * 1e-3)
+    stages = plan.stage_times()
+    info_all = info_dev[args.warmup:].cpu().numpy()
+    fail_rate = float(np.mean(info_all != 0))
+
+    # e2e: the public batched call with host buffers (theta H2D, ll/info D2H)
+    from fgpu import loglik_batch
+    eng_list = [eng] * S
+    loglik_batch(eng_list, list(th_host[0]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        loglik_batch(eng_list, list(th_host[args.warmup + k]))
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if ws > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t)
+    e2e = {"value": S * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": S * nth * 8,
+           "d2h_bytes_per_step": S * (8 + 4)}
+
+    # plain one-particle-per-call drop-in
+    eng.loglik(th_host[0][0])
+    t0 = time.perf_counter()
+    for k in range(args.plain):
+        eng.loglik(th_host[args.warmup][k % S])
+    plain_v = args.plain / (time.perf_counter() - t0)
+
+    plan.set_profiling(False)
+    del plan
+    torch.cuda.empty_cache()
+    peak = fp64_peak_tflops(torch)
+    upd_ms, upd_n = stages["update"]
+    flops = update_flops(p.N, 2) * S
+    achieved = flops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("k_update_bytes_per_launch")
+        except Exception:
+            traffic = None
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+            "kernel": "k_update (FP64 mma.sync m8n8k4 trailing update)",
+            "peak_source": "measured live in this run: cuBLAS DGEMM 8192^3 FP64 (not in MEASURED_PEAKS.json)",
+            "algorithmic_flops_per_step": flops, "launches_per_step": upd_n,
+            "stage_ms_last_step": {k: v[0] for k, v in stages.items()}}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores, model = host_info()
+        sample = args.cpu_sample or cores
+        try:
+            v, dt, _, _ = cpu_baseline(p, mu, sample, cores)
+            cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": f"{sample} particles of the same workload in {dt:.1f} s on {cores} threads ({model}); "
+                             "C restatement of the reference's OpenMP CPU path"}
+        except Exception as exc:  # report, never fall back
+            cpu = {"value": None, "unit": UNIT, "cores": cores, "kind": "port", "sample": f"failed: {exc}"}
+    clocks = clk.summary()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, shapes of the glycine-like config)",
+            "config": {"workload": WORKLOAD, "N": p.N, "d": p.d, "swarm": S, "likelihood": "concentrated",
+                       "kernel": "rbf(17) + periodic(7)", "l2": "inputs larger than L2: 40 K matrices = 5.3 GB "
+                       "written per step", "parallelism": f"replicas x{ws} (independent swarms per GPU)"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": launches_per_step * args.steps,
+            "plain": {"value": plain_v, "unit": UNIT, "particles": args.plain},
+            "batched_over_plain": value / ws / plain_v if plain_v else None,
+            "cholesky_failure_rate": fail_rate}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,671 @@
+// C-ABI of the engine: contexts (one training set each), a per-context pool of
+// workers (stream + workspace + captured CUDA graph) for the plain
+// one-particle-per-call path, and graph-captured batch plans.
+#include "../../include/fgpu.h"
+#include "fgpu_internal.h"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace fgpu;
+
+namespace {
+
+thread_local std::string t_err;
+thread_local long long t_launches = 0;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  t_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(e_ == cudaErrorMemoryAllocation ? FGPU_ENOMEM : FGPU_ECUDA, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                     \
+  } while (0)
+
+int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// Compile the postfix spec into the device-side Spec and the plane list.
+// Returns 0 or an error code (message set).
+int compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>& plane_dim,
+                 std::vector<int>& plane_kind) {
+  memset(&sp, 0, sizeof(sp));
+  int depth = 0, i = 0, param = 0;
+  while (i < nkspec) {
+    const int op = kspec[i];
+    if (op >= FGPU_RBF && op <= FGPU_CONSTANT) {
+      if (i + 1 >= nkspec) return fail(FGPU_EINVAL, "kspec: truncated leaf at %d", i);
+      const int n = kspec[i + 1];
+      if (n < 0 || i + 2 + n > nkspec) return fail(FGPU_EINVAL, "kspec: bad leaf length at %d", i);
+      if (op == FGPU_CONSTANT && n != 0) return fail(FGPU_EINVAL, "kspec: constant leaf takes no dims");
+      if (op != FGPU_CONSTANT && n == 0) return fail(FGPU_EINVAL, "kspec: leaf with no active dims");
+      if (sp.nleaf >= MAX_LEAF) return fail(FGPU_EINVAL, "kspec: more than %d leaves", MAX_LEAF);
+      if (sp.npost >= MAX_POST) return fail(FGPU_EINVAL, "kspec: expression too long");
+      Leaf& L = sp.leaf[sp.nleaf];
+      L.type = op;
+      L.n = n;
+      L.plane0 = (int)plane_dim.size();
+      L.param0 = param;
+      if (op == FGPU_RBF_CYCLIC && n != d)
+        return fail(FGPU_EINVAL,
+                    "kspec: rbf-cyclic needs active dims = all %d features (the reference applies "
+                    "its lengthscale to the whole cyclic distance tensor)", d);
+      for (int k = 0; k < n; ++k) {
+        const int dim = kspec[i + 2 + k];
+        if (dim < 1 || dim > d) return fail(FGPU_EINVAL, "kspec: active dim %d outside 1..%d", dim, d);
+        if (op == FGPU_PERIODIC) {
+          plane_dim.push_back(dim - 1);
+          plane_kind.push_back(1);  // sin(x/2)
+          plane_dim.push_back(dim - 1);
+          plane_kind.push_back(2);  // cos(x/2)
+        } else if (op != FGPU_LINEAR) {
+          plane_dim.push_back(dim - 1);
+          plane_kind.push_back(op == FGPU_RBF_CYCLIC && (dim % 3) == 0 ? 3 : 0);
+        }
+      }
+      param += (op == FGPU_CONSTANT) ? 1 : n;
+      sp.post[sp.npost++] = (int8_t)sp.nleaf;
+      sp.nleaf++;
+      depth++;
+      i += 2 + n;
+    } else if (op == FGPU_SUM || op == FGPU_PROD) {
+      if (depth < 2) return fail(FGPU_EINVAL, "kspec: operator at %d without two operands", i);
+      if (sp.npost >= MAX_POST) return fail(FGPU_EINVAL, "kspec: expression too long");
+      sp.post[sp.npost++] = (op == FGPU_SUM) ? P_SUM : P_PROD;
+      depth--;
+      i += 1;
+    } else {
+      return fail(FGPU_EINVAL, "kspec: bad opcode %d at %d", op, i);
+    }
+  }
+  if (depth != 1) return fail(FGPU_EINVAL, "kspec: does not reduce to one kernel");
+  if ((int)plane_dim.size() > MAX_PLANES)
+    return fail(FGPU_EINVAL, "kspec: %d feature planes exceed the limit %d", (int)plane_dim.size(), MAX_PLANES);
+  if (param > MAX_PARAMS - 1) return fail(FGPU_EINVAL, "kspec: %d parameters exceed the limit", param);
+  sp.nplanes = (int)plane_dim.size();
+  sp.nkparams = param;
+  for (int p = 0; p < sp.nplanes; ++p) sp.cyclic[p] = plane_kind[p] == 3 ? 1 : 0;
+  return 0;
+}
+
+struct Workspace {
+  double* K = nullptr;
+  double* logdet_part = nullptr;
+  int* status = nullptr;
+  double* out = nullptr;
+  double* z = nullptr;
+};
+
+// Optional per-launch event pairs for stage timing (captured into the graph).
+struct StageEvents {
+  std::vector<int> stage;
+  std::vector<cudaEvent_t> ev;  // 2 per launch
+  void clear() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    ev.clear();
+    stage.clear();
+  }
+};
+
+
+}  // namespace
+
+struct Worker {
+  cudaStream_t stream = nullptr;
+  Workspace ws;
+  double* theta_d = nullptr;
+  Prob* prob_d = nullptr;
+  double* h_stage = nullptr;  // pinned: theta | out(4) | status(4 ints as doubles)
+  int* h_status = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  long long graph_kernels = 0;
+  bool busy = false;
+};
+
+struct fgpu_ctx {
+  int device = 0;
+  int N = 0, d = 0, Nc = 0, ld = 0, nsteps = 0, nrhs = 1, likelihood = 0, optimise_noise = 0;
+  int nkparams = 0, ntheta = 0;
+  double noise = 0.0;
+  Spec spec{};
+  Spec* spec_d = nullptr;
+  double* planes_d = nullptr;
+  double* y_d = nullptr;
+  double* mu_d = nullptr;
+  std::mutex mu;
+  std::vector<Worker*> workers;
+};
+
+struct fgpu_plan {
+  int device = 0, nprob = 0, ldtheta = 0, max_nsteps = 0, max_nplanes = 0;
+  std::vector<fgpu_ctx*> ctxs;
+  std::vector<Prob> probs_h;
+  Prob* probs_d = nullptr;
+  double* theta_d = nullptr;
+  double* ll_d = nullptr;
+  int* info_d = nullptr;
+  int* status_all = nullptr;
+  std::vector<void*> allocations;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  long long graph_kernels = 0;
+  double* h_theta = nullptr;
+  double* h_ll = nullptr;
+  int* h_info = nullptr;
+  StageEvents* prof = nullptr;
+  std::mutex mu;
+};
+
+namespace {
+
+size_t K_elems(const fgpu_ctx* c) { return (size_t)c->ld * c->Nc; }
+
+void fill_prob(Prob& p, const fgpu_ctx* c, const double* theta_d, const Workspace& ws) {
+  memset(&p, 0, sizeof(p));
+  p.N = c->N;
+  p.Nc = c->Nc;
+  p.ld = c->ld;
+  p.nsteps = c->nsteps;
+  p.nrhs = c->nrhs;
+  p.likelihood = c->likelihood;
+  p.optimise_noise = c->optimise_noise;
+  p.nkparams = c->nkparams;
+  p.noise = c->noise;
+  p.planes = c->planes_d;
+  p.y = c->y_d;
+  p.mu = c->mu_d;
+  p.spec = c->spec_d;
+  p.theta = theta_d;
+  p.K = ws.K;
+  p.logdet_part = ws.logdet_part;
+  p.status = ws.status;
+  p.out = ws.out;
+  p.z = ws.z;
+}
+
+int mark(StageEvents* pe, int stage, cudaStream_t s, bool begin) {
+  if (!pe) return 0;
+  cudaEvent_t e;
+  CK(cudaEventCreate(&e));
+  pe->ev.push_back(e);
+  if (begin) pe->stage.push_back(stage);
+  // External: becomes an event-record node of the captured graph
+  CK(cudaEventRecordWithFlags(e, s, cudaEventRecordExternal));
+  return 0;
+}
+
+#define STAGE(st, call)                        \
+  do {                                         \
+    int r_ = mark(pe, st, s, true);            \
+    if (r_) return r_;                         \
+    CK(call);                                  \
+    r_ = mark(pe, st, s, false);               \
+    if (r_) return r_;                         \
+    ++n;                                       \
+  } while (0)
+
+// Enqueue the whole evaluation: reset, build, sweep, epilogue.
+int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes, int* status_base,
+                 size_t status_bytes, cudaStream_t s, long long* kernels, StageEvents* pe) {
+  long long n = 0;
+  CK(cudaMemsetAsync(status_base, 0, status_bytes, s));
+  STAGE(0, launch_build(probs_d, nprob, max_nsteps, max_nplanes, s));
+  for (int step = 0; step < max_nsteps; ++step) {
+    STAGE(1, launch_potf2(probs_d, nprob, step, s));
+    STAGE(2, launch_trsm(probs_d, nprob, step, max_nsteps, s));
+    if (max_nsteps - step - 1 > 0) STAGE(3, launch_update(probs_d, nprob, step, max_nsteps, s));
+  }
+  STAGE(4, launch_finalize(probs_d, nprob, s));
+  if (kernels) *kernels = n;
+  return 0;
+}
+
+int capture(cudaStream_t s, cudaGraphExec_t* exec, const Prob* probs_d, int nprob, int max_nsteps,
+            int max_nplanes, int* status_base, size_t status_bytes, long long* kernels,
+            StageEvents* pe = nullptr) {
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_eval(probs_d, nprob, max_nsteps, max_nplanes, status_base, status_bytes, s, kernels, pe);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (rc != 0) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(FGPU_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(FGPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  return 0;
+}
+
+int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track) {
+  CK(cudaMalloc(&ws.K, K_elems(c) * sizeof(double)));
+  CK(cudaMalloc(&ws.logdet_part, sizeof(double) * (c->nsteps + 1)));
+  CK(cudaMalloc(&ws.out, sizeof(double) * 8));
+  CK(cudaMalloc(&ws.z, sizeof(double) * c->Nc));
+  if (track) {
+    track->push_back(ws.K);
+    track->push_back(ws.logdet_part);
+    track->push_back(ws.out);
+    track->push_back(ws.z);
+  }
+  return 0;
+}
+
+void free_worker(Worker* w) {
+  if (!w) return;
+  if (w->graph) cudaGraphExecDestroy(w->graph);
+  cudaFree(w->ws.K);
+  cudaFree(w->ws.logdet_part);
+  cudaFree(w->ws.status);
+  cudaFree(w->ws.out);
+  cudaFree(w->ws.z);
+  cudaFree(w->theta_d);
+  cudaFree(w->prob_d);
+  if (w->h_stage) cudaFreeHost(w->h_stage);
+  if (w->stream) cudaStreamDestroy(w->stream);
+  delete w;
+}
+
+int make_worker(fgpu_ctx* c, Worker** out) {
+  Worker* w = new (std::nothrow) Worker();
+  if (!w) return fail(FGPU_ENOMEM, "worker allocation");
+  int rc = 0;
+  auto bail = [&](int r) {
+    free_worker(w);
+    return r;
+  };
+  if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(FGPU_ECUDA, "stream create failed"));
+  if ((rc = alloc_workspace(c, w->ws, nullptr)) != 0) return bail(rc);
+  if (cudaMalloc(&w->ws.status, sizeof(int) * 4) != cudaSuccess) return bail(fail(FGPU_ENOMEM, "status alloc"));
+  if (cudaMalloc(&w->theta_d, sizeof(double) * (c->ntheta + 1)) != cudaSuccess)
+    return bail(fail(FGPU_ENOMEM, "theta alloc"));
+  if (cudaMalloc(&w->prob_d, sizeof(Prob)) != cudaSuccess) return bail(fail(FGPU_ENOMEM, "desc alloc"));
+  if (cudaMallocHost(&w->h_stage, sizeof(double) * (c->ntheta + 16)) != cudaSuccess)
+    return bail(fail(FGPU_ENOMEM, "pinned alloc"));
+  w->h_status = reinterpret_cast<int*>(w->h_stage + c->ntheta + 8);
+  Prob p;
+  fill_prob(p, c, w->theta_d, w->ws);
+  if (cudaMemcpy(w->prob_d, &p, sizeof(Prob), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(FGPU_ECUDA, "desc copy"));
+  if ((rc = capture(w->stream, &w->graph, w->prob_d, 1, c->nsteps, c->spec.nplanes, w->ws.status,
+                    sizeof(int) * 4, &w->graph_kernels)) != 0)
+    return bail(rc);
+  *out = w;
+  return 0;
+}
+
+Worker* acquire(fgpu_ctx* c, int* rc) {
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    for (Worker* w : c->workers)
+      if (!w->busy) {
+        w->busy = true;
+        return w;
+      }
+  }
+  Worker* w = nullptr;
+  *rc = make_worker(c, &w);
+  if (*rc) return nullptr;
+  std::lock_guard<std::mutex> lk(c->mu);
+  w->busy = true;
+  c->workers.push_back(w);
+  return w;
+}
+
+void release(fgpu_ctx* c, Worker* w) {
+  std::lock_guard<std::mutex> lk(c->mu);
+  w->busy = false;
+}
+
+std::mutex g_plan_mu;
+std::map<std::vector<fgpu_ctx*>, fgpu_plan*> g_plans;
+
+}  // namespace
+
+extern "C" {
+
+const char* fgpu_last_error(void) { return t_err.c_str(); }
+const char* fgpu_version(void) { return "fgpu 0.1 sm_103a fp64"; }
+long long fgpu_last_launch_count(void) { return t_launches; }
+
+int fgpu_create(fgpu_ctx** out, int N, int d, const double* X, const double* y, const double* mu,
+                const int* kspec, int nkspec, int likelihood, double noise, int optimise_noise) {
+  t_err.clear();
+  if (!out) return fail(FGPU_EINVAL, "ctx pointer is NULL");
+  *out = nullptr;
+  if (N < 1 || d < 1) return fail(FGPU_EINVAL, "N=%d d=%d must be positive", N, d);
+  if (!X || !y || !kspec || nkspec < 1) return fail(FGPU_EINVAL, "NULL input array");
+  if (likelihood != FGPU_MARGINAL && likelihood != FGPU_CONCENTRATED)
+    return fail(FGPU_EINVAL, "likelihood %d is neither marginal (0) nor concentrated (1)", likelihood);
+  if (likelihood == FGPU_MARGINAL && !mu) return fail(FGPU_EINVAL, "marginal likelihood needs mu");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(FGPU_ENODEV, "no CUDA device");
+  std::unique_ptr<fgpu_ctx> c(new (std::nothrow) fgpu_ctx());
+  if (!c) return fail(FGPU_ENOMEM, "context allocation");
+  CK(cudaGetDevice(&c->device));
+  std::vector<int> plane_dim, plane_kind;
+  int rc = compile_spec(kspec, nkspec, d, c->spec, plane_dim, plane_kind);
+  if (rc) return rc;
+  c->N = N;
+  c->d = d;
+  c->Nc = round_up(N, TB);
+  c->ld = c->Nc + TB;
+  c->nsteps = c->Nc / TB;
+  c->likelihood = likelihood;
+  c->nrhs = likelihood == FGPU_CONCENTRATED ? 2 : 1;
+  c->noise = noise;
+  c->optimise_noise = optimise_noise ? 1 : 0;
+  c->nkparams = c->spec.nkparams;
+  c->ntheta = c->nkparams + c->optimise_noise;
+  // feature planes, plane-major, padded to Nc
+  const int np = c->spec.nplanes;
+  std::vector<double> planes((size_t)std::max(np, 1) * c->Nc, 0.0);
+  for (int p = 0; p < np; ++p) {
+    const double* col = X + (size_t)plane_dim[p] * N;  // X(:, dim), column-major
+    double* dst = planes.data() + (size_t)p * c->Nc;
+    for (int i = 0; i < N; ++i) {
+      const double x = col[i];
+      if (plane_kind[p] == 1)
+        dst[i] = std::sin(x / 2.0);
+      else if (plane_kind[p] == 2)
+        dst[i] = std::cos(x / 2.0);
+      else
+        dst[i] = x;
+    }
+  }
+  std::vector<double> yv(c->Nc, 0.0), mv(c->Nc, 0.0);
+  for (int i = 0; i < N; ++i) {
+    yv[i] = y[i];
+    mv[i] = mu ? mu[i] : 0.0;
+  }
+  CK(cudaMalloc(&c->planes_d, planes.size() * sizeof(double)));
+  CK(cudaMemcpy(c->planes_d, planes.data(), planes.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&c->y_d, c->Nc * sizeof(double)));
+  CK(cudaMemcpy(c->y_d, yv.data(), c->Nc * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&c->mu_d, c->Nc * sizeof(double)));
+  CK(cudaMemcpy(c->mu_d, mv.data(), c->Nc * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&c->spec_d, sizeof(Spec)));
+  CK(cudaMemcpy(c->spec_d, &c->spec, sizeof(Spec), cudaMemcpyHostToDevice));
+  *out = c.release();
+  return 0;
+}
+
+int fgpu_nparams(const fgpu_ctx* ctx) { return ctx ? ctx->ntheta : FGPU_EINVAL; }
+
+void fgpu_destroy(fgpu_ctx* ctx) {
+  if (!ctx) return;
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    for (auto it = g_plans.begin(); it != g_plans.end();) {
+      bool uses = false;
+      for (fgpu_ctx* c : it->first) uses |= (c == ctx);
+      if (uses) {
+        fgpu_plan_destroy(it->second);
+        it = g_plans.erase(it);
+      } else {
+        ++it;
+      }
+    }
+  }
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(ctx->device);
+  for (Worker* w : ctx->workers) free_worker(w);
+  cudaFree(ctx->planes_d);
+  cudaFree(ctx->y_d);
+  cudaFree(ctx->mu_d);
+  cudaFree(ctx->spec_d);
+  cudaSetDevice(prev);
+  delete ctx;
+}
+
+int fgpu_loglik(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, int* info, double* alpha) {
+  t_err.clear();
+  t_launches = 0;
+  if (!ctx || !theta || !ll || !info) return fail(FGPU_EINVAL, "NULL argument");
+  if (ntheta != ctx->ntheta) return fail(FGPU_EINVAL, "ntheta=%d, context expects %d", ntheta, ctx->ntheta);
+  for (int k = 0; k < ntheta; ++k)
+    if (!std::isfinite(theta[k])) return fail(FGPU_EINVAL, "theta[%d] is not finite", k);
+  CK(cudaSetDevice(ctx->device));
+  int rc = 0;
+  Worker* w = acquire(ctx, &rc);
+  if (!w) return rc;
+  struct Rel {
+    fgpu_ctx* c;
+    Worker* w;
+    ~Rel() { release(c, w); }
+  } rel{ctx, w};
+  memcpy(w->h_stage, theta, sizeof(double) * ntheta);
+  CK(cudaMemcpyAsync(w->theta_d, w->h_stage, sizeof(double) * ntheta, cudaMemcpyHostToDevice, w->stream));
+  CK(cudaGraphLaunch(w->graph, w->stream));
+  t_launches = w->graph_kernels;
+  if (alpha) {
+    CK(launch_backsolve(w->prob_d, 1, ctx->nsteps, nullptr, w->stream, &t_launches));
+  }
+  double* h_out = w->h_stage + ctx->ntheta;
+  CK(cudaMemcpyAsync(h_out, w->ws.out, sizeof(double) * 4, cudaMemcpyDeviceToHost, w->stream));
+  CK(cudaMemcpyAsync(w->h_status, w->ws.status, sizeof(int) * 4, cudaMemcpyDeviceToHost, w->stream));
+  if (alpha) CK(cudaMemcpyAsync(alpha, w->ws.z, sizeof(double) * ctx->N, cudaMemcpyDeviceToHost, w->stream));
+  CK(cudaStreamSynchronize(w->stream));
+  if (w->h_status[2]) return fail(FGPU_ETIMEOUT, "bulk copy into shared memory did not complete");
+  *info = w->h_status[0];
+  *ll = (*info == 0) ? h_out[0] : std::nan("");
+  return 0;
+}
+
+int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, double* dll, int* info) {
+  (void)ctx;
+  (void)theta;
+  (void)ntheta;
+  (void)ll;
+  (void)dll;
+  (void)info;
+  return fail(FGPU_EINVAL, "fgpu_grad: adjoint not available in this build");
+}
+
+int fgpu_plan_create(fgpu_plan** out, fgpu_ctx* const* ctxs, int nprob, int ldtheta) {
+  t_err.clear();
+  if (!out || !ctxs || nprob < 1) return fail(FGPU_EINVAL, "bad plan arguments");
+  *out = nullptr;
+  std::unique_ptr<fgpu_plan> p(new (std::nothrow) fgpu_plan());
+  if (!p) return fail(FGPU_ENOMEM, "plan allocation");
+  p->nprob = nprob;
+  p->device = ctxs[0]->device;
+  int maxth = 0;
+  for (int i = 0; i < nprob; ++i) {
+    if (!ctxs[i]) return fail(FGPU_EINVAL, "ctxs[%d] is NULL", i);
+    if (ctxs[i]->device != p->device) return fail(FGPU_EINVAL, "plan spans devices");
+    maxth = std::max(maxth, ctxs[i]->ntheta);
+    p->max_nsteps = std::max(p->max_nsteps, ctxs[i]->nsteps);
+    p->max_nplanes = std::max(p->max_nplanes, ctxs[i]->spec.nplanes);
+    p->ctxs.push_back(ctxs[i]);
+  }
+  if (ldtheta < maxth) return fail(FGPU_EINVAL, "ldtheta=%d < max nparams %d", ldtheta, maxth);
+  p->ldtheta = ldtheta;
+  CK(cudaSetDevice(p->device));
+  auto track = [&](void* q) { p->allocations.push_back(q); };
+  CK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  CK(cudaMalloc(&p->theta_d, sizeof(double) * (size_t)nprob * ldtheta));
+  track(p->theta_d);
+  CK(cudaMalloc(&p->ll_d, sizeof(double) * nprob));
+  track(p->ll_d);
+  CK(cudaMalloc(&p->info_d, sizeof(int) * nprob));
+  track(p->info_d);
+  CK(cudaMalloc(&p->status_all, sizeof(int) * 4 * nprob));
+  track(p->status_all);
+  CK(cudaMalloc(&p->probs_d, sizeof(Prob) * nprob));
+  track(p->probs_d);
+  CK(cudaMallocHost(&p->h_theta, sizeof(double) * (size_t)nprob * ldtheta));
+  CK(cudaMallocHost(&p->h_ll, sizeof(double) * nprob));
+  CK(cudaMallocHost(&p->h_info, sizeof(int) * nprob));
+  p->probs_h.resize(nprob);
+  for (int i = 0; i < nprob; ++i) {
+    Workspace ws;
+    int rc = alloc_workspace(ctxs[i], ws, &p->allocations);
+    if (rc) {
+      fgpu_plan_destroy(p.release());
+      return rc;
+    }
+    ws.status = p->status_all + 4 * i;
+    fill_prob(p->probs_h[i], ctxs[i], p->theta_d + (size_t)i * ldtheta, ws);
+    p->probs_h[i].ll_dst = p->ll_d + i;
+    p->probs_h[i].info_dst = p->info_d + i;
+  }
+  CK(cudaMemcpy(p->probs_d, p->probs_h.data(), sizeof(Prob) * nprob, cudaMemcpyHostToDevice));
+  int rc = capture(p->stream, &p->graph, p->probs_d, nprob, p->max_nsteps, p->max_nplanes, p->status_all,
+                   sizeof(int) * 4 * nprob, &p->graph_kernels);
+  if (rc) {
+    fgpu_plan_destroy(p.release());
+    return rc;
+  }
+  *out = p.release();
+  return 0;
+}
+
+void fgpu_plan_destroy(fgpu_plan* p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  if (p->graph) cudaGraphExecDestroy(p->graph);
+  if (p->prof) {
+    p->prof->clear();
+    delete p->prof;
+  }
+  for (void* q : p->allocations) cudaFree(q);
+  if (p->h_theta) cudaFreeHost(p->h_theta);
+  if (p->h_ll) cudaFreeHost(p->h_ll);
+  if (p->h_info) cudaFreeHost(p->h_info);
+  if (p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+}
+
+int fgpu_plan_set_profiling(fgpu_plan* p, int enable) {
+  t_err.clear();
+  if (!p) return fail(FGPU_EINVAL, "plan is NULL");
+  CK(cudaSetDevice(p->device));
+  std::lock_guard<std::mutex> lk(p->mu);
+  CK(cudaStreamSynchronize(p->stream));
+  if (p->prof) {
+    p->prof->clear();
+    delete p->prof;
+    p->prof = nullptr;
+  }
+  if (enable) p->prof = new StageEvents();
+  cudaGraphExec_t g = nullptr;
+  long long nk = 0;
+  int rc = capture(p->stream, &g, p->probs_d, p->nprob, p->max_nsteps, p->max_nplanes, p->status_all,
+                   sizeof(int) * 4 * p->nprob, &nk, p->prof);
+  if (rc) return rc;
+  if (p->graph) cudaGraphExecDestroy(p->graph);
+  p->graph = g;
+  p->graph_kernels = nk;
+  return 0;
+}
+
+int fgpu_plan_stage_times(fgpu_plan* p, double* ms, int* count) {
+  t_err.clear();
+  if (!p || !ms || !count) return fail(FGPU_EINVAL, "NULL argument");
+  if (!p->prof) return fail(FGPU_EINVAL, "profiling is not enabled on this plan");
+  CK(cudaSetDevice(p->device));
+  for (int k = 0; k < FGPU_NSTAGES; ++k) {
+    ms[k] = 0.0;
+    count[k] = 0;
+  }
+  for (size_t i = 0; i < p->prof->stage.size(); ++i) {
+    float t = 0.f;
+    CK(cudaEventSynchronize(p->prof->ev[2 * i + 1]));
+    CK(cudaEventElapsedTime(&t, p->prof->ev[2 * i], p->prof->ev[2 * i + 1]));
+    ms[p->prof->stage[i]] += t;
+    count[p->prof->stage[i]] += 1;
+  }
+  return 0;
+}
+
+int fgpu_plan_run_device(fgpu_plan* p, const double* theta_dev, double* ll_dev, int* info_dev, void* stream) {
+  t_err.clear();
+  if (!p) return fail(FGPU_EINVAL, "plan is NULL");
+  CK(cudaSetDevice(p->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (theta_dev && theta_dev != p->theta_d)
+    CK(cudaMemcpyAsync(p->theta_d, theta_dev, sizeof(double) * (size_t)p->nprob * p->ldtheta,
+                       cudaMemcpyDeviceToDevice, s));
+  CK(cudaGraphLaunch(p->graph, s));
+  t_launches = p->graph_kernels;
+  if (ll_dev && ll_dev != p->ll_d)
+    CK(cudaMemcpyAsync(ll_dev, p->ll_d, sizeof(double) * p->nprob, cudaMemcpyDeviceToDevice, s));
+  if (info_dev && info_dev != p->info_d)
+    CK(cudaMemcpyAsync(info_dev, p->info_d, sizeof(int) * p->nprob, cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+int fgpu_plan_run(fgpu_plan* p, const double* theta_host, double* ll_host, int* info_host) {
+  t_err.clear();
+  if (!p || !theta_host || !ll_host || !info_host) return fail(FGPU_EINVAL, "NULL argument");
+  CK(cudaSetDevice(p->device));
+  std::lock_guard<std::mutex> lk(p->mu);
+  const size_t tb = sizeof(double) * (size_t)p->nprob * p->ldtheta;
+  memcpy(p->h_theta, theta_host, tb);
+  CK(cudaMemcpyAsync(p->theta_d, p->h_theta, tb, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaGraphLaunch(p->graph, p->stream));
+  t_launches = p->graph_kernels;
+  CK(cudaMemcpyAsync(p->h_ll, p->ll_d, sizeof(double) * p->nprob, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaMemcpyAsync(p->h_info, p->info_d, sizeof(int) * p->nprob, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  memcpy(ll_host, p->h_ll, sizeof(double) * p->nprob);
+  memcpy(info_host, p->h_info, sizeof(int) * p->nprob);
+  for (int i = 0; i < p->nprob; ++i)
+    if (info_host[i] < 0) return fail(FGPU_ETIMEOUT, "problem %d: bulk copy did not complete", i);
+  return 0;
+}
+
+int fgpu_loglik_batch(fgpu_ctx* const* ctxs, int nprob, const double* const* theta, double* ll, int* info) {
+  t_err.clear();
+  if (!ctxs || !theta || !ll || !info || nprob < 1) return fail(FGPU_EINVAL, "bad batch arguments");
+  std::vector<fgpu_ctx*> key(ctxs, ctxs + nprob);
+  int maxth = 0;
+  for (int i = 0; i < nprob; ++i) {
+    if (!ctxs[i] || !theta[i]) return fail(FGPU_EINVAL, "NULL entry %d", i);
+    maxth = std::max(maxth, ctxs[i]->ntheta);
+  }
+  fgpu_plan* p = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_plans.find(key);
+    if (it != g_plans.end()) p = it->second;
+  }
+  if (!p) {
+    int rc = fgpu_plan_create(&p, ctxs, nprob, std::max(maxth, 1));
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    g_plans[key] = p;
+  }
+  std::vector<double> th((size_t)nprob * p->ldtheta, 0.0);
+  for (int i = 0; i < nprob; ++i) {
+    for (int k = 0; k < ctxs[i]->ntheta; ++k) {
+      if (!std::isfinite(theta[i][k])) return fail(FGPU_EINVAL, "theta[%d][%d] is not finite", i, k);
+      th[(size_t)i * p->ldtheta + k] = theta[i][k];
+    }
+  }
+  return fgpu_plan_run(p, th.data(), ll, info);
+}
+
+}  // extern "C"

@@ -1,0 +1,596 @@
+// FP64 engine kernels: kernel-matrix build, blocked right-looking Cholesky
+// (diagonal factor, panel solve, trailing update on the FP64 MMA pipe),
+// likelihood epilogue and the back-substitution for alpha.
+//
+// Every kernel takes the device array of problem descriptors and indexes it
+// by blockIdx.z (tile kernels) or blockIdx.x (per-problem kernels), so one
+// launch serves a whole ragged batch.
+#include "fgpu_internal.h"
+
+#include <cmath>
+#include <cstdio>
+
+namespace fgpu {
+
+#define FGPU_PI 3.141592653589793115997963468544185161590576171875
+#define FGPU_TWOPI 6.28318530717958623199592693708837032318115234375
+#define FGPU_LOG_TWOPI 1.8378770664093453390819377091247588396072387695312
+
+// ---------------------------------------------------------------------------
+// small PTX helpers: mbarrier + bulk async copy (the TMA engine's 1-D form)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: returns false if the barrier did not complete within the limit.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// kernel-matrix build
+// ---------------------------------------------------------------------------
+// Raw parameters -> stored kernel parameters (rbf_kernel.f90:113-119,
+// periodic_kernel.f90:111-118, rbf_cyclic_kernel.f90:109-115,
+// linear_kernel.f90:94-100, constant.f90:86-90).
+__device__ __forceinline__ double transform_param(int type, double t) {
+  switch (type) {
+    case L_RBF:
+    case L_RBF_CYCLIC:
+      return exp(t);
+    case L_PERIODIC: {
+      double l = 1.0 / exp(t);
+      return l * l;
+    }
+    case L_LINEAR:
+      return exp(-t);
+    default:
+      return t;
+  }
+}
+
+// One leaf at one (i, j) pair.  Pi / Pj point at the row / column tile's
+// planes in shared memory (plane p of point r at P[p * TB + r]).
+__device__ __forceinline__ double leaf_value(const Leaf& L, const double* __restrict__ Pi,
+                                             const double* __restrict__ Pj, int ri, int cj,
+                                             const double* __restrict__ ls, const uint8_t* cyc,
+                                             double lin_sum) {
+  const int p0 = L.plane0, q0 = L.param0, n = L.n;
+  switch (L.type) {
+    case L_RBF: {
+      // stationary_kernel.f90:101-122: exp(-0.5 * sum_k l_k (x_ik - x_jk)^2)
+      double acc = 0.0;
+      for (int k = 0; k < n; ++k) {
+        double dlt = Pi[(p0 + k) * TB + ri] - Pj[(p0 + k) * TB + cj];
+        acc = fma(ls[q0 + k], dlt * dlt, acc);
+      }
+      return exp(-0.5 * acc);
+    }
+    case L_PERIODIC: {
+      // periodic_kernel.f90:181-206 on distance_matrix.f90:130-142:
+      // exp(-2 * sum_k l_k sin^2(|x_ik - x_jk| / 2)), with
+      // sin((a-b)/2) = sin(a/2)cos(b/2) - cos(a/2)sin(b/2).
+      double acc = 0.0;
+      for (int k = 0; k < n; ++k) {
+        const double si = Pi[(p0 + 2 * k) * TB + ri], ci = Pi[(p0 + 2 * k + 1) * TB + ri];
+        const double sj = Pj[(p0 + 2 * k) * TB + cj], cjv = Pj[(p0 + 2 * k + 1) * TB + cj];
+        double t = fma(si, cjv, -(ci * sj));
+        acc = fma(ls[q0 + k], t * t, acc);
+      }
+      return exp(-2.0 * acc);
+    }
+    case L_RBF_CYCLIC: {
+      // stationary_cyclic_kernel.f90:104-127 on distance_matrix.f90:95-128:
+      // every 3rd feature's difference wrapped to [-pi, pi].
+      double acc = 0.0;
+      for (int k = 0; k < n; ++k) {
+        double dlt = Pi[(p0 + k) * TB + ri] - Pj[(p0 + k) * TB + cj];
+        if (cyc[p0 + k]) {
+          double a = fabs(dlt) + FGPU_PI;
+          dlt = copysign(1.0, dlt) * (fmod(a, FGPU_TWOPI) - FGPU_PI);
+        }
+        acc = fma(ls[q0 + k], dlt * dlt, acc);
+      }
+      return exp(-0.5 * acc);
+    }
+    case L_LINEAR:
+      // linear_kernel.f90:70-76 with the reference's default order 0:
+      // sum_k (x_ik x_jk)^0 / c_k, independent of (i, j).
+      return lin_sum;
+    default:
+      return ls[q0];  // constant.f90:62-68
+  }
+}
+
+__device__ __forceinline__ double kernel_value(const Spec& sp, const double* Pi, const double* Pj, int ri,
+                                               int cj, const double* ls, const double* lin_sums) {
+  double stk[MAX_LEAF];
+  int top = 0;
+  for (int t = 0; t < sp.npost; ++t) {
+    const int tok = sp.post[t];
+    if (tok >= 0) {
+      stk[top++] = leaf_value(sp.leaf[tok], Pi, Pj, ri, cj, ls, sp.cyclic, lin_sums[tok]);
+    } else {
+      const double b = stk[--top];
+      const double a = stk[--top];
+      stk[top++] = (tok == P_SUM) ? a + b : a * b;  // kernel_module.f90:309-325 / 359-375
+    }
+  }
+  return stk[0];
+}
+
+size_t build_smem_bytes(int nplanes) {
+  return (size_t)2 * nplanes * TB * sizeof(double) + 64;
+}
+
+// grid: (row tile 0..nsteps, col tile 0..nsteps-1, problem); 256 threads.
+// Each thread produces 2 consecutive rows x 8 columns of the 64 x 64 tile and
+// writes them as double2 so that a warp stores 512 contiguous bytes.
+__global__ void __launch_bounds__(256) k_build(const Prob* __restrict__ probs) {
+  const Prob& P = probs[blockIdx.z];
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (tj >= P.nsteps || ti > P.nsteps || ti < tj) return;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const Spec& sp = *P.spec;
+  const int np = sp.nplanes;
+  double* Pi = reinterpret_cast<double*>(smem_raw);
+  double* Pj = Pi + (size_t)np * TB;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(Pj + (size_t)np * TB);
+  __shared__ double ls[MAX_PARAMS];
+  __shared__ double lin_sums[MAX_LEAF];
+  __shared__ int s_fail;
+
+  const int tid = threadIdx.x;
+  const bool border = (ti == P.nsteps);
+  const int i0 = ti * TB, j0 = tj * TB;
+
+  if (tid == 0) {
+    s_fail = 0;
+    if (np > 0) {
+      mbar_init(bar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && np > 0) {
+    const uint32_t per = TB * sizeof(double);
+    const uint32_t total = per * np * (border ? 1 : 2);
+    mbar_arrive_expect_tx(bar, total);
+    for (int p = 0; p < np; ++p) {
+      bulk_g2s(Pj + p * TB, P.planes + (size_t)p * P.Nc + j0, per, bar);
+      if (!border) bulk_g2s(Pi + p * TB, P.planes + (size_t)p * P.Nc + i0, per, bar);
+    }
+  }
+  // parameters while the copies fly
+  for (int k = tid; k < sp.nkparams; k += blockDim.x) {
+    int type = L_CONSTANT;
+    for (int l = 0; l < sp.nleaf; ++l) {
+      const int cnt = sp.leaf[l].type == L_CONSTANT ? 1 : sp.leaf[l].n;
+      if (k >= sp.leaf[l].param0 && k < sp.leaf[l].param0 + cnt) type = sp.leaf[l].type;
+    }
+    ls[k] = transform_param(type, P.theta[k]);
+  }
+  __syncthreads();
+  if (tid < sp.nleaf) {
+    double s = 0.0;
+    const Leaf& L = sp.leaf[tid];
+    if (L.type == L_LINEAR)
+      for (int k = 0; k < L.n; ++k) s += 1.0 / ls[L.param0 + k];
+    lin_sums[tid] = s;
+  }
+  if (np > 0 && !mbar_wait_bounded(bar, 0)) s_fail = 1;
+  __syncthreads();
+  if (s_fail) {
+    if (tid == 0) atomicExch(&P.status[2], 1);  // copy engine did not answer: report, do not hang
+    return;
+  }
+
+  const double noise = P.optimise_noise ? P.theta[sp.nkparams] : P.noise;
+  const int r0 = (tid & 31) * 2;
+  const int c0 = (tid >> 5) * 8;
+  double* K = P.K;
+  const size_t ld = (size_t)P.ld;
+  for (int cc = 0; cc < 8; ++cc) {
+    const int c = c0 + cc, j = j0 + c;
+    double v[2];
+    for (int a = 0; a < 2; ++a) {
+      const int r = r0 + a, i = i0 + r;
+      double val = 0.0;
+      if (border) {
+        const int q = r;
+        if (j < P.N && q < P.nrhs) {
+          if (q == 0)
+            val = (P.likelihood == 1) ? P.y[j] : P.y[j] - P.mu[j];
+          else
+            val = 1.0;
+        }
+      } else if (i < P.N && j < P.N) {
+        if (i >= j) {
+          val = kernel_value(sp, Pi, Pj, r, c, ls, lin_sums);
+          if (i == j) val = val + noise * 1.0;  // gpr.f90:188, nugget * identity
+        }
+      } else {
+        val = (i == j) ? 1.0 : 0.0;  // identity padding
+      }
+      v[a] = val;
+    }
+    *reinterpret_cast<double2*>(K + (size_t)j * ld + i0 + r0) = make_double2(v[0], v[1]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// diagonal block factorisation (unblocked, right-looking) + log-det partial
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_potf2(const Prob* __restrict__ probs, int step) {
+  const Prob& P = probs[blockIdx.x];
+  if (step >= P.nsteps) return;
+  if (*(volatile int*)&P.status[1]) return;
+  __shared__ double A[TB * (TB + 1)];
+  __shared__ double rdiag;
+  __shared__ int fail_col;
+  const int tid = threadIdx.x;
+  const size_t ld = (size_t)P.ld;
+  double* Kd = P.K + (size_t)(step * TB) * ld + step * TB;
+  for (int e = tid; e < TB * TB; e += blockDim.x) {
+    const int r = e % TB, c = e / TB;
+    A[c * (TB + 1) + r] = Kd[(size_t)c * ld + r];
+  }
+  if (tid == 0) fail_col = -1;
+  __syncthreads();
+  for (int j = 0; j < TB; ++j) {
+    if (tid == 0) {
+      const double d = A[j * (TB + 1) + j];
+      if (!(d > 0.0)) {
+        fail_col = j;
+      } else {
+        const double s = sqrt(d);
+        A[j * (TB + 1) + j] = s;
+        rdiag = 1.0 / s;
+      }
+    }
+    __syncthreads();
+    if (fail_col >= 0) break;
+    if (tid > j && tid < TB) A[j * (TB + 1) + tid] *= rdiag;
+    __syncthreads();
+    const int w = TB - 1 - j;  // trailing order
+    for (int e = tid; e < w * w; e += blockDim.x) {
+      const int r = j + 1 + e % w, c = j + 1 + e / w;
+      if (r >= c) A[c * (TB + 1) + r] = fma(-A[j * (TB + 1) + r], A[j * (TB + 1) + c], A[c * (TB + 1) + r]);
+    }
+    __syncthreads();
+  }
+  if (fail_col >= 0) {
+    if (tid == 0) {
+      P.status[0] = step * TB + fail_col + 1;  // LAPACK info: 1-based column
+      P.status[1] = 1;
+    }
+    return;
+  }
+  for (int e = tid; e < TB * TB; e += blockDim.x) {
+    const int r = e % TB, c = e / TB;
+    if (r >= c) Kd[(size_t)c * ld + r] = A[c * (TB + 1) + r];
+  }
+  // log-det partial: 2 * sum log(L_jj) is formed in the epilogue
+  // (arith.f90:72-93); here the block's sum of logs, in column order.
+  if (tid < 32) {
+    double s = log(A[(2 * tid) * (TB + 1) + 2 * tid]) + log(A[(2 * tid + 1) * (TB + 1) + 2 * tid + 1]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (tid == 0) P.logdet_part[step] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// panel solve: A21 <- A21 * L11^-T for the row tiles below the diagonal block
+// (including the border tile of right-hand sides)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_trsm(const Prob* __restrict__ probs, int step) {
+  const Prob& P = probs[blockIdx.y];
+  const int ti = step + 1 + blockIdx.x;
+  if (step >= P.nsteps || ti > P.nsteps) return;
+  if (*(volatile int*)&P.status[1]) return;
+  __shared__ double L[TB * (TB + 1)];
+  __shared__ double B[TB * (TB + 1)];
+  __shared__ double rd[TB];
+  const int tid = threadIdx.x;
+  const size_t ld = (size_t)P.ld;
+  const double* Ld = P.K + (size_t)(step * TB) * ld + step * TB;
+  double* Bd = P.K + (size_t)(step * TB) * ld + ti * TB;
+  for (int e = tid; e < TB * TB; e += blockDim.x) {
+    const int r = e % TB, c = e / TB;
+    L[c * (TB + 1) + r] = Ld[(size_t)c * ld + r];
+    B[c * (TB + 1) + r] = Bd[(size_t)c * ld + r];
+  }
+  __syncthreads();
+  if (tid < TB) rd[tid] = 1.0 / L[tid * (TB + 1) + tid];
+  __syncthreads();
+  for (int c = 0; c < TB; ++c) {
+    if (tid < TB) B[c * (TB + 1) + tid] *= rd[c];
+    __syncthreads();
+    const int w = TB - 1 - c;
+    for (int e = tid; e < w * TB; e += blockDim.x) {
+      const int r = e % TB, q = c + 1 + e / TB;
+      B[q * (TB + 1) + r] = fma(-B[c * (TB + 1) + r], L[c * (TB + 1) + q], B[q * (TB + 1) + r]);
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < TB * TB; e += blockDim.x) {
+    const int r = e % TB, c = e / TB;
+    Bd[(size_t)c * ld + r] = B[c * (TB + 1) + r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// trailing update C(ti, tj) -= P(ti) P(tj)^T on the FP64 MMA pipe
+// (mma.sync m8n8k4 f64).  128 threads, 4 warps x (32 x 32).
+// ---------------------------------------------------------------------------
+constexpr int UPD_STRIDE = TB + 8;  // k-major staging, 8-double pad
+
+__device__ __forceinline__ void dmma_8x8x4(double& c0, double& c1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+               : "+d"(c0), "+d"(c1)
+               : "d"(a), "d"(b));
+}
+
+__global__ void __launch_bounds__(128) k_update(const Prob* __restrict__ probs, int step) {
+  const Prob& P = probs[blockIdx.z];
+  const int ti = step + 1 + blockIdx.x, tj = step + 1 + blockIdx.y;
+  if (step >= P.nsteps || tj >= P.nsteps || ti > P.nsteps || ti < tj) return;
+  if (*(volatile int*)&P.status[1]) return;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* As = reinterpret_cast<double*>(smem_raw);  // [k][m]
+  double* Bs = As + TB * UPD_STRIDE;                  // [k][n]
+  const int tid = threadIdx.x;
+  const size_t ld = (size_t)P.ld;
+  const double* Ag = P.K + (size_t)(step * TB) * ld + ti * TB;
+  const double* Bg = P.K + (size_t)(step * TB) * ld + tj * TB;
+  // 64 columns x 64 rows each; a warp moves one column (32 x double2) per pass
+  for (int e = tid; e < TB * (TB / 2); e += blockDim.x) {
+    const int k = e / (TB / 2), m2 = (e % (TB / 2)) * 2;
+    const double2 a = *reinterpret_cast<const double2*>(Ag + (size_t)k * ld + m2);
+    const double2 b = *reinterpret_cast<const double2*>(Bg + (size_t)k * ld + m2);
+    *reinterpret_cast<double2*>(As + k * UPD_STRIDE + m2) = a;
+    *reinterpret_cast<double2*>(Bs + k * UPD_STRIDE + m2) = b;
+  }
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  double acc[4][4][2];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b][0] = acc[a][b][1] = 0.0;
+  const int lr = lane >> 2, lk = lane & 3;
+#pragma unroll 2
+  for (int k0 = 0; k0 < TB; k0 += 4) {
+    double af[4], bf[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) af[a] = As[(k0 + lk) * UPD_STRIDE + wm + a * 8 + lr];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) bf[b] = Bs[(k0 + lk) * UPD_STRIDE + wn + b * 8 + lr];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) dmma_8x8x4(acc[a][b][0], acc[a][b][1], af[a], bf[b]);
+  }
+  double* Cg = P.K + (size_t)(tj * TB) * ld + ti * TB;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int m = wm + a * 8 + lr;
+      const int n = wn + b * 8 + lk * 2;
+      double* c0p = Cg + (size_t)n * ld + m;
+      double* c1p = Cg + (size_t)(n + 1) * ld + m;
+      *c0p = *c0p - acc[a][b][0];
+      *c1p = *c1p - acc[a][b][1];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// likelihood epilogue (likelihood.f90:161-253) from the border rows
+// ---------------------------------------------------------------------------
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+  __syncthreads();
+  if (threadIdx.x == 0) red[0] = s;
+  __syncthreads();
+  return red[0];
+}
+
+__global__ void __launch_bounds__(256) k_finalize(const Prob* __restrict__ probs) {
+  const Prob& P = probs[blockIdx.x];
+  __shared__ double red[32];
+  const int tid = threadIdx.x;
+  const int N = P.N;
+  if (P.status[1] || P.status[2]) {
+    if (tid == 0) {
+      const int info = P.status[2] ? -1 : P.status[0];
+      P.out[0] = nan("");
+      P.status[0] = info;
+      if (P.ll_dst) *P.ll_dst = nan("");
+      if (P.info_dst) *P.info_dst = info;
+    }
+    return;
+  }
+  const size_t ld = (size_t)P.ld;
+  const double* z0 = P.K + P.Nc;      // row Nc: r_0 = y - mu (marginal) or y (concentrated)
+  const double* z1 = P.K + P.Nc + 1;  // row Nc+1: ones (concentrated)
+  double logdet = 0.0;
+  if (tid == 0) {
+    for (int s = 0; s < P.nsteps; ++s) logdet += P.logdet_part[s];
+    logdet *= 2.0;
+  }
+  double ll, mean = 0.0, s2 = 0.0;
+  if (P.likelihood == 0) {
+    double q = 0.0;
+    for (int j = tid; j < N; j += blockDim.x) {
+      const double v = z0[(size_t)j * ld];
+      q = fma(v, v, q);
+      P.z[j] = v;
+    }
+    q = block_sum(q, red);
+    ll = -0.5 * q - 0.5 * logdet - 0.5 * (double)N * FGPU_LOG_TWOPI;
+  } else {
+    double a = 0.0, b = 0.0;
+    for (int j = tid; j < N; j += blockDim.x) {
+      const double u = z0[(size_t)j * ld], v = z1[(size_t)j * ld];
+      a = fma(v, u, a);
+      b = fma(v, v, b);
+    }
+    a = block_sum(a, red);
+    b = block_sum(b, red);
+    mean = a / b;  // 1^T K^-1 y / 1^T K^-1 1 (likelihood.f90:229)
+    double q = 0.0;
+    for (int j = tid; j < N; j += blockDim.x) {
+      const double w = z0[(size_t)j * ld] - mean * z1[(size_t)j * ld];
+      q = fma(w, w, q);
+      P.z[j] = w;
+    }
+    q = block_sum(q, red);
+    s2 = q / (double)N;  // (y - mu)^T K^-1 (y - mu) / N (likelihood.f90:239)
+    ll = -0.5 * (double)N * log(s2) - 0.5 * logdet;
+  }
+  for (int j = N + tid; j < P.Nc; j += blockDim.x) P.z[j] = 0.0;
+  if (tid == 0) {
+    P.out[0] = ll;
+    P.out[1] = logdet;
+    P.out[2] = mean;
+    P.out[3] = s2;
+    P.status[0] = 0;
+    if (P.ll_dst) *P.ll_dst = ll;
+    if (P.info_dst) *P.info_dst = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// alpha = L^-T z by blocked back-substitution (dpotrs's second half)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(TB) k_bs_diag(const Prob* __restrict__ probs, int blk) {
+  const Prob& P = probs[blockIdx.x];
+  if (blk >= P.nsteps || P.status[1] || P.status[2]) return;
+  __shared__ double L[TB * (TB + 1)];
+  __shared__ double z[TB];
+  const int tid = threadIdx.x;
+  const size_t ld = (size_t)P.ld;
+  const double* Ld = P.K + (size_t)(blk * TB) * ld + blk * TB;
+  for (int c = 0; c < TB; ++c) L[c * (TB + 1) + tid] = Ld[(size_t)c * ld + tid];
+  z[tid] = P.z[blk * TB + tid];
+  __syncthreads();
+  for (int c = TB - 1; c >= 0; --c) {
+    if (tid == 0) z[c] = z[c] / L[c * (TB + 1) + c];
+    __syncthreads();
+    if (tid < c) z[tid] = fma(-L[tid * (TB + 1) + c], z[c], z[tid]);
+    __syncthreads();
+  }
+  P.z[blk * TB + tid] = z[tid];
+}
+
+// z[0 : blk*TB) -= L[blk rows, 0 : blk*TB)^T alpha_blk; one warp per column.
+__global__ void __launch_bounds__(256) k_bs_update(const Prob* __restrict__ probs, int blk) {
+  const Prob& P = probs[blockIdx.y];
+  if (blk >= P.nsteps || P.status[1] || P.status[2]) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int col = blockIdx.x * 8 + warp;
+  if (col >= blk * TB) return;
+  const size_t ld = (size_t)P.ld;
+  const double* Lc = P.K + (size_t)col * ld + blk * TB;
+  const double* ab = P.z + blk * TB;
+  double s = fma(Lc[lane], ab[lane], Lc[lane + 32] * ab[lane + 32]);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) P.z[col] -= s;
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+static int g_build_attr_set = 0, g_update_attr_set = 0;
+
+cudaError_t launch_build(const Prob* probs, int nprob, int max_nsteps, int max_nplanes, cudaStream_t s) {
+  const size_t smem = build_smem_bytes(max_nplanes);
+  if (!g_build_attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)build_smem_bytes(MAX_PLANES));
+    if (e != cudaSuccess) return e;
+    g_build_attr_set = 1;
+  }
+  dim3 grid(max_nsteps + 1, max_nsteps, nprob);
+  k_build<<<grid, 256, smem, s>>>(probs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s) {
+  k_potf2<<<nprob, 256, 0, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s) {
+  const int rows = max_nsteps - step;  // row tiles step+1 .. nsteps (incl. border)
+  if (rows <= 0) return cudaSuccess;
+  k_trsm<<<dim3(rows, nprob), 256, 0, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s) {
+  const int m = max_nsteps - step - 1;  // trailing column tiles
+  if (m <= 0) return cudaSuccess;
+  const int smem = 2 * TB * UPD_STRIDE * (int)sizeof(double);
+  if (!g_update_attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_update, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    g_update_attr_set = 1;
+  }
+  k_update<<<dim3(m + 1, m, nprob), 128, smem, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const Prob* probs, int nprob, cudaStream_t s) {
+  k_finalize<<<nprob, 256, 0, s>>>(probs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_backsolve(const Prob* probs, int nprob, int max_nsteps, double* /*alpha_out*/,
+                             cudaStream_t s, long long* nlaunch) {
+  for (int b = max_nsteps - 1; b >= 0; --b) {
+    k_bs_diag<<<nprob, TB, 0, s>>>(probs, b);
+    if (nlaunch) ++*nlaunch;
+    if (b > 0) {
+      k_bs_update<<<dim3((b * TB + 7) / 8, nprob), 256, 0, s>>>(probs, b);
+      if (nlaunch) ++*nlaunch;
+    }
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace fgpu

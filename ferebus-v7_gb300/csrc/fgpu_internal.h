@@ -1,0 +1,79 @@
+// Internal declarations shared by the engine's translation units.
+//
+// Data layout in HBM (one problem = one training set evaluated at one theta):
+//
+//   planes  : nplanes x Nc doubles, plane-major.  One plane per (leaf, active
+//             dim): x for rbf / rbf-cyclic / linear, and the pair
+//             sin(x/2), cos(x/2) for periodic, so that
+//             sin((xi-xj)/2) = s_i c_j - c_i s_j needs no FP64 sin per pair.
+//   K       : ld x Nc, column-major (Fortran order, like the reference's
+//             covariance_matrix).  Nc = N rounded up to TB; ld = Nc + TB.
+//             Rows [0, N) x cols [0, N): k(X, X) + nugget (lower triangle).
+//             Rows/cols [N, Nc): identity padding, so every panel is full.
+//             Rows [Nc, Nc + nrhs): the right-hand sides r_q^T (border rows);
+//             the Cholesky sweep turns them into (L^-1 r_q)^T, which is all
+//             the log-likelihood needs.  Rows [Nc + nrhs, ld): zero.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace fgpu {
+
+constexpr int TB = 64;            // panel width and tile edge
+constexpr int MAX_LEAF = 8;
+constexpr int MAX_POST = 16;
+constexpr int MAX_PLANES = 192;
+constexpr int MAX_PARAMS = 256;
+constexpr int MAX_RHS = 2;
+
+enum LeafType { L_RBF = 1, L_PERIODIC = 2, L_RBF_CYCLIC = 3, L_LINEAR = 4, L_CONSTANT = 5 };
+enum PostTok : int8_t { P_SUM = -1, P_PROD = -2 };
+
+struct Leaf {
+  int type;     // LeafType
+  int n;        // active dims (0 for constant)
+  int plane0;   // first plane of this leaf
+  int param0;   // first kernel parameter of this leaf
+};
+
+struct Spec {
+  int nleaf;
+  Leaf leaf[MAX_LEAF];
+  int npost;
+  int8_t post[MAX_POST];          // >= 0: leaf index; P_SUM / P_PROD
+  int nplanes;
+  int nkparams;
+  uint8_t cyclic[MAX_PLANES];     // rbf-cyclic: plane's feature index is 3, 6, 9, ... (1-based)
+};
+
+// Per-problem descriptor, resident in device memory.
+struct Prob {
+  int N, Nc, ld, nsteps, nrhs, likelihood, optimise_noise, nkparams;
+  double noise;
+  const double* planes;           // nplanes x Nc
+  const double* y;                // Nc, zero padded
+  const double* mu;               // Nc, zero padded (marginal)
+  const Spec* spec;
+  const double* theta;            // raw parameters
+  double* K;                      // ld x Nc
+  double* logdet_part;            // nsteps
+  int* status;                    // [0] info (LAPACK convention), [1] failed flag
+  double* out;                    // [0] ll, [1] logdet, [2] mean, [3] sigma2
+  double* z;                      // Nc: the vector alpha's back-substitution starts from
+  double* ll_dst;                 // optional extra destination for ll (batch output)
+  int* info_dst;                  // optional extra destination for info
+};
+
+// Launch helpers (engine.cu).  All kernels take a device array of problems
+// and index it by blockIdx.y; problems whose geometry does not reach the
+// current step exit immediately, so ragged batches share one launch.
+cudaError_t launch_build(const Prob* probs, int nprob, int max_nsteps, int max_nplanes, cudaStream_t s);
+cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s);
+cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s);
+cudaError_t launch_update(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s);
+cudaError_t launch_finalize(const Prob* probs, int nprob, cudaStream_t s);
+cudaError_t launch_backsolve(const Prob* probs, int nprob, int max_nsteps, double* alpha_out,
+                             cudaStream_t s, long long* nlaunch);
+size_t build_smem_bytes(int nplanes);
+
+}  // namespace fgpu

@@ -1,0 +1,135 @@
+/*
+ * fgpu.h -- C-ABI of the GB300 GPR log-likelihood engine.
+ *
+ * Drop-in for the likelihood evaluation that FEREBUS-v7's particle swarm runs
+ * once per particle: kernel matrix K(theta) + nugget, Cholesky, log-det,
+ * alpha = K^-1 (y - mu), marginal or concentrated log-likelihood.
+ *
+ * Conventions (ISO_C_BINDING compatible: plain pointers and scalars only)
+ *  - Arrays are FP64 and column-major exactly as Fortran stores them:
+ *    X(N, d) is DataSet%x%data (src/csv.f90:37-177, src/data/data_input.f90:34).
+ *  - theta is the reference's raw parameter vector: kernel parameters in
+ *    kernel-tree order (src/kernels/kernel_module.f90:235-245) followed, when
+ *    optimise_noise is set, by the LINEAR noise value (src/model/gpr/gpr.f90:191-202).
+ *    The engine applies exp(theta) (rbf, rbf-cyclic), exp(-theta)^2 (periodic),
+ *    exp(-theta) (linear) and the identity (constant) itself.
+ *  - Return value: 0 on success, < 0 on an argument / CUDA / allocation error
+ *    (fgpu_last_error() has the message).  A non-positive-definite K is NOT
+ *    an error: the call returns 0 and sets info > 0 to the 1-based column of
+ *    the first non-positive pivot, as LAPACK dpotrf does
+ *    (src/model/gpr/likelihood.f90:130-159); the host maps info != 0 to
+ *    IterResult%success = .false. (src/optimiser/iter_result.f90:92-101).
+ *  - No entry point aborts the process.
+ */
+#ifndef FGPU_H
+#define FGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Kernel-spec opcodes.  kspec is the postfix flattening of the kernel
+ * expression tree built by the reference's KernelInterpreter
+ * (src/interpreter/kernel_interpreter.f90:43-69, ast.f90:173-271):
+ * a leaf is {op, n_active, dim_1 .. dim_n} with 1-based feature indices
+ * (TOML active_dimensions), an operator is {op}.  A constant leaf is
+ * {FGPU_CONSTANT, 0} and owns one parameter. */
+#define FGPU_RBF 1
+#define FGPU_PERIODIC 2
+#define FGPU_RBF_CYCLIC 3
+#define FGPU_LINEAR 4
+#define FGPU_CONSTANT 5
+#define FGPU_SUM 10
+#define FGPU_PROD 11
+
+#define FGPU_MARGINAL 0
+#define FGPU_CONCENTRATED 1
+
+/* Error codes (negative return values). */
+#define FGPU_OK 0
+#define FGPU_EINVAL (-1)
+#define FGPU_ECUDA (-2)
+#define FGPU_ENOMEM (-3)
+#define FGPU_ENODEV (-4)
+#define FGPU_ETIMEOUT (-5)
+
+typedef struct fgpu_ctx fgpu_ctx;     /* one training set on one device */
+typedef struct fgpu_plan fgpu_plan;   /* a fixed batch of problems, graph-captured */
+
+/* Create a context for one training set.  Replaces the per-GPR set-up of
+ * GaussianProcessRegressor%init (src/model/gpr/gpr.f90:124-183) and the
+ * distance-tensor precompute (src/kernels/distance_matrix.f90:48-62,
+ * called at app/main.f90:108).  X, y and mu are copied to the device once;
+ * mu is the cached mean vector (gpr.f90:171) and is ignored (may be NULL)
+ * for the concentrated likelihood.  Create it once per training set, not
+ * once per particle. */
+int fgpu_create(fgpu_ctx** ctx, int N, int d, const double* X, const double* y,
+                const double* mu, const int* kspec, int nkspec, int likelihood,
+                double noise, int optimise_noise);
+
+/* Number of entries theta must hold (GaussianProcessRegressor%nparams, gpr.f90:248-256). */
+int fgpu_nparams(const fgpu_ctx* ctx);
+
+/* Plain drop-in: one particle per call.  Replaces
+ * GaussianProcessRegressor%log_likelihood (src/model/gpr/gpr.f90:291-307) ->
+ * compute_R (gpr.f90:185-189) + Likelihood%ll (src/model/gpr/likelihood.f90:161-253).
+ * alpha (length N, may be NULL) receives K^-1 (y - mu) (the [weights] of the
+ * model file, likelihood.f90:255-264).  Thread-safe: concurrent calls on one
+ * context each take their own stream and workspace from the context's pool. */
+int fgpu_loglik(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, int* info,
+                double* alpha);
+
+/* Batched: nprob problems (any mix of contexts -- atoms, properties, particles;
+ * ragged N and d) evaluated as one graph-captured pass.  Replaces the OpenMP
+ * particle loop of global_swarm_update (src/optimiser/pso/pso.f90:419-452)
+ * and init_pso (pso.f90:294-308).  theta[p] points at problem p's raw
+ * parameters.  The plan for a given context list is built on first use and
+ * cached. */
+int fgpu_loglik_batch(fgpu_ctx* const* ctxs, int nprob, const double* const* theta,
+                      double* ll, int* info);
+
+/* Log-likelihood and its gradient d logL / d theta (including the noise
+ * parameter when optimise_noise is set) by the FP64 adjoint
+ * 1/2 tr((alpha alpha^T / s - K^-1) dK/dtheta), s = 1 (marginal) or sigma^2
+ * (concentrated).  The reference has no analytic likelihood gradient
+ * (negative_log_likelihood, gpr.f90:258-289, accepts but ignores
+ * gradient=.true.); this is the optional gradient polish.  dll_dtheta has
+ * fgpu_nparams(ctx) entries. */
+int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll,
+              double* dll_dtheta, int* info);
+
+/* Device-resident batch plan (inputs and outputs stay in HBM).  theta_dev is
+ * nprob x ldtheta doubles on the device; ll_dev / info_dev are device arrays of
+ * nprob entries.  stream is a cudaStream_t (NULL = the plan's own stream).
+ * Used by the throughput benchmark and by hosts that keep the swarm on the GPU. */
+int fgpu_plan_create(fgpu_plan** plan, fgpu_ctx* const* ctxs, int nprob, int ldtheta);
+int fgpu_plan_run_device(fgpu_plan* plan, const double* theta_dev, double* ll_dev,
+                         int* info_dev, void* stream);
+int fgpu_plan_run(fgpu_plan* plan, const double* theta_host, double* ll_host,
+                  int* info_host);
+void fgpu_plan_destroy(fgpu_plan* plan);
+
+void fgpu_destroy(fgpu_ctx* ctx);
+
+/* Stage timing for roofline accounting.  When enabled, the plan's graph is
+ * re-captured with CUDA event nodes around every launch; after a run,
+ * fgpu_plan_stage_times fills ms[k] with the summed device time of stage k
+ * during the LAST replay and count[k] with its launches (k: 0 build,
+ * 1 diagonal factor, 2 panel solve, 3 trailing update, 4 likelihood
+ * epilogue).  Diagnostic only; the reference has no counterpart. */
+#define FGPU_NSTAGES 5
+int fgpu_plan_set_profiling(fgpu_plan* plan, int enable);
+int fgpu_plan_stage_times(fgpu_plan* plan, double* ms, int* count);
+
+/* Thread-local message for the last failing call on this thread. */
+const char* fgpu_last_error(void);
+
+/* Engine version string and the number of kernel launches the last call on
+ * this thread enqueued (graph replays count their nodes). */
+const char* fgpu_version(void);
+long long fgpu_last_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FGPU_H */

@@ -1,0 +1,189 @@
+"""GPU parity: the CUDA engine (through the C-ABI) against the CPU oracle.
+
+Tolerance on the log-likelihood: max(1e-9 * |ll|, 4 * spread), where
+``spread`` is the case's measured LAPACK-to-LAPACK difference (OpenBLAS
+dpotrf/dpotrs vs MKL) for the same K.  Where K is well conditioned the
+spread is ~1e-15 relative and the bar is the 1e-9 relative target; for the
+ill-conditioned water-like sets (nugget 1e-10, cond(K) ~ 1e12) no two LAPACKs
+agree to 1e-9 and the bar is their own disagreement.
+"""
+import math
+import threading
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_case
+from oracle import gpr_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def tol(ll, spread):
+    return max(1e-9 * abs(ll), 4.0 * spread)
+
+
+def engine_for(c):
+    from fgpu import Engine
+    return Engine(c["X"], c["y"], c["mu"], [int(v) for v in c["kspec"]], int(c["likelihood"]),
+                  float(c["noise"]), bool(c["optimise_noise"]))
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_golden_loglik(name, lib):
+    c = load_case(name)
+    e = engine_for(c)
+    for k, th in enumerate(c["thetas"]):
+        ll, info = e.loglik(th)
+        if c["info"][k] != 0:
+            assert info > 0 and math.isnan(ll)
+            assert info >= c["info"][k] - 1
+        else:
+            assert info == 0, (k, info)
+            assert abs(ll - c["ll"][k]) <= tol(c["ll"][k], c["spread"][k]), (k, ll, c["ll"][k])
+
+
+@pytest.mark.parametrize("name", [n for n in golden_cases() if "not_pd" not in n])
+def test_golden_alpha_is_a_backward_stable_solve(name, lib):
+    """alpha = K^-1 r: ||K alpha - r|| <= 1e-12 ||K|| ||alpha|| (conditioning-free),
+    and close to the oracle's alpha where K is well conditioned."""
+    c = load_case(name)
+    e = engine_for(c)
+    th = c["thetas"][0]
+    ll, info, alpha = e.loglik(th, want_alpha=True)
+    assert info == 0
+    ks = [int(v) for v in c["kspec"]]
+    nk = O.kernel_nparams(ks)
+    noise = float(th[nk]) if int(c["optimise_noise"]) else float(c["noise"])
+    K = O.compute_R(ks, th[:nk], noise, O.Tensors(c["X"], need_cyclic=O.RBF_CYCLIC in ks))
+    K = np.tril(K) + np.tril(K, -1).T
+    if int(c["likelihood"]) == 0:
+        r = c["y"] - c["mu"]
+    else:
+        res = O.loglik(ks, th, c["X"], c["y"], c["mu"], 1, float(c["noise"]), bool(c["optimise_noise"]), want=True)
+        r = c["y"] - res["mean"]
+    resid = np.linalg.norm(K @ alpha - r)
+    assert resid <= 1e-12 * np.linalg.norm(K, 2) * np.linalg.norm(alpha) + 1e-14 * np.linalg.norm(r)
+    if c["spread"][0] <= 1e-12 * abs(c["ll"][0]):
+        ref = c["alpha0"]
+        assert np.linalg.norm(alpha - ref) <= 1e-7 * np.linalg.norm(ref)
+
+
+def _random_problem(n, d, lik, seed, kernel="rbf+per"):
+    rng = np.random.default_rng(seed)
+    X = rng.normal(2.0, 0.3, size=(n, d))
+    X[:, -1] = rng.uniform(-np.pi, np.pi, size=n)
+    y = np.cos(X[:, 0]) + 0.2 * np.sin(X[:, -1]) + 1e-3 * rng.normal(size=n)
+    if kernel == "rbf+per":
+        ks = [O.RBF, d - 1] + list(range(1, d)) + [O.PERIODIC, 1, d, O.SUM]
+    else:
+        ks = [O.RBF, d] + list(range(1, d + 1))
+    mu = O.mean_vector("constant", X, y)
+    th = rng.uniform(0.0, 1.0, size=O.kernel_nparams(ks))
+    return X, y, mu, ks, th
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 63, 64, 65, 127, 128, 129, 200])
+@pytest.mark.parametrize("lik", [0, 1])
+def test_edge_sizes_against_oracle(n, lik, lib):
+    from fgpu import Engine
+    X, y, mu, ks, th = _random_problem(n, 4, lik, seed=n * 7 + lik)
+    noise = 1e-6
+    e = Engine(X, y, mu, ks, lik, noise, False)
+    ll, info = e.loglik(th)
+    ref, rinfo = O.loglik(ks, th, X, y, mu, lik, noise, False)
+    assert info == rinfo == 0
+    if n == 1 and lik == 1:
+        # one point: the profiled variance is 0 up to rounding (y - mu is 0 or
+        # a few ulp), so ll = -N/2 log(sigma^2) is +inf or a large positive
+        # number depending on the last bit in either implementation
+        assert ll > 30 and ref > 30
+    else:
+        assert abs(ll - ref) <= 1e-9 * abs(ref) + 1e-12, (ll, ref)
+
+
+def test_ragged_batch_equals_plain_calls(lib):
+    from fgpu import Engine, loglik_batch
+    engines, thetas = [], []
+    for k, (n, d, lik) in enumerate([(70, 3, 0), (130, 5, 1), (64, 4, 0), (1, 2, 0), (257, 6, 1)]):
+        X, y, mu, ks, th = _random_problem(n, d, lik, seed=100 + k)
+        engines.append(Engine(X, y, mu, ks, lik, 1e-6, False))
+        thetas.append(th)
+    probs = [engines[i % 5] for i in range(12)]
+    ths = [thetas[i % 5] + 0.01 * (i // 5) for i in range(12)]
+    ll, info = loglik_batch(probs, ths)
+    for i in range(12):
+        l1, i1 = probs[i].loglik(ths[i])
+        assert info[i] == i1 == 0
+        assert ll[i] == l1  # same kernels, same tiles: bitwise equal
+    ll2, _ = loglik_batch(probs, ths)   # cached plan, replayed graph
+    assert np.array_equal(ll, ll2)
+
+
+def test_plan_device_entry_point(lib):
+    torch = pytest.importorskip("torch")
+    from fgpu import Engine, Plan
+    X, y, mu, ks, th = _random_problem(150, 4, 0, seed=5)
+    e = Engine(X, y, mu, ks, 0, 1e-6, False)
+    plan = Plan([e] * 3)
+    th3 = torch.tensor(np.stack([th, th * 0.9, th * 1.1]), dtype=torch.float64, device="cuda")
+    ll = torch.empty(3, dtype=torch.float64, device="cuda")
+    info = torch.empty(3, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream()
+    plan.run_device(th3.data_ptr(), ll.data_ptr(), info.data_ptr(), s.cuda_stream)
+    torch.cuda.synchronize()
+    for k in range(3):
+        l1, i1 = e.loglik(th3[k].cpu().numpy())
+        assert int(info[k]) == i1 == 0 and float(ll[k]) == l1
+
+
+def test_concurrent_calls_on_one_context(lib):
+    from fgpu import Engine
+    X, y, mu, ks, th = _random_problem(300, 5, 0, seed=9)
+    e = Engine(X, y, mu, ks, 0, 1e-6, False)
+    thetas = [th + 0.02 * k for k in range(8)]
+    want = [e.loglik(t)[0] for t in thetas]
+    got = [None] * 8
+
+    def work(k):
+        got[k] = e.loglik(thetas[k])[0]
+
+    ts = [threading.Thread(target=work, args=(k,)) for k in range(8)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert got == want
+
+
+def test_invalid_theta_is_an_error_not_a_fault(lib):
+    from fgpu import Engine
+    from fgpu._lib import FgpuError
+    X, y, mu, ks, th = _random_problem(40, 3, 0, seed=3)
+    e = Engine(X, y, mu, ks, 0, 1e-6, False)
+    bad = th.copy()
+    bad[0] = np.nan
+    with pytest.raises(FgpuError):
+        e.loglik(bad)
+    with pytest.raises(FgpuError):
+        e.loglik(th[:-1])
+    assert e.loglik(th)[1] == 0  # context still usable
+
+
+def test_full_size_glycine_like_config(lib):
+    """N=4000, d=24 (the benchmark workload): batch of particles == plain calls,
+    and one particle against the oracle."""
+    from fgpu import Engine, loglik_batch
+    from fgpu import synth
+    p = synth.config3()
+    mu = O.mean_vector("constant", p.X, p.y)
+    e = Engine(p.X, p.y, mu, p.kspec, p.likelihood, p.noise, p.optimise_noise)
+    th = p.thetas(3)
+    ll, info = loglik_batch([e] * 3, list(th))
+    for k in range(3):
+        l1, i1 = e.loglik(th[k])
+        assert info[k] == i1 and ll[k] == l1
+    ref, rinfo = O.loglik(p.kspec, th[0], p.X, p.y, mu, p.likelihood, p.noise, False,
+                          tens=O.Tensors(p.X, lazy=True))
+    assert rinfo == info[0] == 0
+    assert abs(ll[0] - ref) <= 1e-9 * abs(ref)
