@@ -669,3 +669,19 @@ int fgpu_loglik_batch(fgpu_ctx* const* ctxs, int nprob, const double* const* the
 }
 
 }  // extern "C"
+
+// Hooks for other translation units of the library: the spec compiler and the
+// thread-local error channel behind fgpu_last_error().
+namespace fgpu {
+int internal_compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>& plane_dim,
+                          std::vector<int>& plane_kind) {
+  t_err.clear();
+  return compile_spec(kspec, nkspec, d, sp, plane_dim, plane_kind);
+}
+int internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+void internal_clear_error() {
+  t_err.clear();
+  t_launches = 0;
+}
+void internal_add_launches(long long n) { t_launches += n; }
+}  // namespace fgpu

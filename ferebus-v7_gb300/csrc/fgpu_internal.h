@@ -16,6 +16,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <vector>
 
 namespace fgpu {
 
@@ -75,5 +76,12 @@ cudaError_t launch_finalize(const Prob* probs, int nprob, cudaStream_t s);
 cudaError_t launch_backsolve(const Prob* probs, int nprob, int max_nsteps, double* alpha_out,
                              cudaStream_t s, long long* nlaunch);
 size_t build_smem_bytes(int nplanes);
+
+// api.cu hooks for other translation units.
+int internal_compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>& plane_dim,
+                          std::vector<int>& plane_kind);
+int internal_fail(int code, const char* msg);
+void internal_clear_error();
+void internal_add_launches(long long n);
 
 }  // namespace fgpu

@@ -18,7 +18,7 @@ EXPORTS = (
     "fgpu_create", "fgpu_nparams", "fgpu_loglik", "fgpu_loglik_batch", "fgpu_grad",
     "fgpu_plan_create", "fgpu_plan_run_device", "fgpu_plan_run", "fgpu_plan_destroy",
     "fgpu_destroy", "fgpu_last_error", "fgpu_version", "fgpu_last_launch_count",
-    "fgpu_plan_set_profiling", "fgpu_plan_stage_times",
+    "fgpu_plan_set_profiling", "fgpu_plan_stage_times", "fgpu_loglik_noalloc",
 )
 
 c_double_p = C.POINTER(C.c_double)
@@ -74,6 +74,9 @@ def load(path=None):
     lib.fgpu_plan_set_profiling.restype = C.c_int
     lib.fgpu_plan_stage_times.argtypes = [vp, c_double_p, c_int_p]
     lib.fgpu_plan_stage_times.restype = C.c_int
+    lib.fgpu_loglik_noalloc.argtypes = [C.c_int, C.c_int, vp, vp, vp, c_int_p, C.c_int, C.c_int, C.c_double,
+                                        C.c_int, vp, vp, vp, vp]
+    lib.fgpu_loglik_noalloc.restype = C.c_int
     _lib = lib
     return lib
 

@@ -111,6 +111,28 @@ void fgpu_plan_destroy(fgpu_plan* plan);
 
 void fgpu_destroy(fgpu_ctx* ctx);
 
+/* One evaluation that allocates no device memory.  No counterpart in the
+ * reference: it exists for hosts that may not call cudaMalloc when they need
+ * a likelihood (device memory owned by an OpenACC runtime's data regions or
+ * by a pool that forbids side allocations; a thread evaluating while a
+ * global-mode stream capture is active elsewhere in the process).  Inputs
+ * (X(N,d) column-major, y, mu, theta) and outputs (ll, info: one value each)
+ * are DEVICE pointers; kspec is host memory.  All intermediates live in one
+ * fixed static device array (about 9.5 MB per device, held until the process
+ * exits), so N <= FGPU_NOALLOC_MAX_N and the kernel spec may need at most
+ * FGPU_NOALLOC_MAX_PLANES feature planes (one per rbf dim, two per periodic
+ * dim); larger inputs are rejected with FGPU_EINVAL.  The work is enqueued on
+ * `stream` (a cudaStream_t, NULL = legacy default) and the call returns
+ * without waiting.  The first call on a device resolves the array's address
+ * (cudaGetSymbolAddress) -- make it before any stream capture.  Every call
+ * shares the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
+#define FGPU_NOALLOC_MAX_N 1024
+#define FGPU_NOALLOC_MAX_PLANES 64
+int fgpu_loglik_noalloc(int N, int d, const double* X_dev, const double* y_dev, const double* mu_dev,
+                        const int* kspec, int nkspec, int likelihood, double noise, int optimise_noise,
+                        const double* theta_dev, double* ll_dev, int* info_dev, void* stream);
+
 /* Stage timing for roofline accounting.  When enabled, the plan's graph is
  * re-captured with CUDA event nodes around every launch; after a run,
  * fgpu_plan_stage_times fills ms[k] with the summed device time of stage k
