@@ -121,6 +121,17 @@ def update_flops(N, nrhs, tb=64):
     return tot
 
 
+def tensor_update_flops(N, nslice=7, nb=128, tn=64):
+    """fp16 tensor-core flops the split-integer trailing update issues for one
+    factorisation: per step s, m(m+1) output tiles of nb x tn (m trailing
+    128-row tiles), each nb*tn*nb multiply-adds per digit pair, and
+    nslice(nslice+1)/2 digit pairs."""
+    nt = -(-N // nb)
+    pairs = nslice * (nslice + 1) // 2
+    tiles = sum((nt - s - 1) * (nt - s) for s in range(nt))
+    return 2.0 * nb * tn * nb * pairs * tiles
+
+
 def fp64_peak_tflops(torch):
     """Live FP64 peak: cuBLAS DGEMM 8192^3, best of 3."""
     n = 8192
@@ -216,6 +227,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=0, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--trailing", default="tcgen05", choices=("tcgen05", "fp64"),
+                    help="trailing-update arithmetic of the Cholesky")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -231,8 +244,10 @@ def main():
 
     from fgpu import Engine, Plan, synth
     from fgpu.build import build_library
-    from fgpu.gpr import mean_vector
+    from fgpu.gpr import mean_vector, set_trailing_update
     build_library()
+    mode = args.trailing
+    set_trailing_update(mode)
 
     p = synth.config3()
     mu = mean_vector(p.mean, p.X, p.y)
@@ -305,23 +320,42 @@ def main():
     plan.set_profiling(False)
     del plan
     torch.cuda.empty_cache()
-    peak = fp64_peak_tflops(torch)
+    fp64_peak = fp64_peak_tflops(torch)
     upd_ms, upd_n = stages["update"]
-    flops = update_flops(p.N, 2) * S
-    achieved = flops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
+    fp64_flops = update_flops(p.N, 0 if mode == "tcgen05" else 2, tb=128 if mode == "tcgen05" else 64) * S
+    fp64_equiv = fp64_flops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
     traffic = None
     tf = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tf):
         try:
-            traffic = json.load(open(tf)).get("k_update_bytes_per_launch")
+            traffic = json.load(open(tf)).get(f"k_update_bytes_per_launch_{mode}")
         except Exception:
             traffic = None
-    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-            "kernel": "k_update (FP64 mma.sync m8n8k4 trailing update)",
-            "peak_source": "measured live in this run: cuBLAS DGEMM 8192^3 FP64 (not in MEASURED_PEAKS.json)",
-            "algorithmic_flops_per_step": flops, "launches_per_step": upd_n,
-            "stage_ms_last_step": {k: v[0] for k, v in stages.items()}}
+    stage_ms = {k: v[0] for k, v in stages.items() if v[1]}
+    if mode == "tcgen05":
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        tpeak = peaks.get("bf16_tflops_sustained")
+        src = "MEASURED_PEAKS.json bf16_tflops_sustained (dense fp16/bf16 tensor, kernel timed inside a long step)"
+        if not tpeak:
+            tpeak, src = 1700.0, "fallback: 1.7 PFLOP/s sustained bf16 (profiling recipe)"
+        tflops = tensor_update_flops(p.N) * S
+        achieved = tflops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
+        roof = {"bound": "tensor", "achieved": achieved, "peak": tpeak, "unit": "TFLOP/s",
+                "frac": (achieved / tpeak) if achieved else None, "traffic": traffic,
+                "kernel": "k_ozaki_update (tcgen05.mma kind::f16, 7 fp16 digit planes, exact int64 accumulation)",
+                "peak_source": src, "tensor_flops_per_step": tflops, "launches_per_step": upd_n,
+                "fp64_equivalent": {"achieved": fp64_equiv, "fp64_peak": fp64_peak, "unit": "TFLOP/s",
+                                    "ratio": (fp64_equiv / fp64_peak) if fp64_equiv else None,
+                                    "fp64_peak_source": "measured live: cuBLAS DGEMM 8192^3"},
+                "stage_ms_last_step": stage_ms}
+    else:
+        roof = {"bound": "tensor", "achieved": fp64_equiv, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": (fp64_equiv / fp64_peak) if fp64_equiv else None, "traffic": traffic,
+                "kernel": "k_update (FP64 mma.sync m8n8k4 trailing update)",
+                "peak_source": "measured live in this run: cuBLAS DGEMM 8192^3 FP64 (not in MEASURED_PEAKS.json)",
+                "algorithmic_flops_per_step": fp64_flops, "launches_per_step": upd_n,
+                "stage_ms_last_step": stage_ms}
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores, model = host_info()
@@ -338,6 +372,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, shapes of the glycine-like config)",
             "config": {"workload": WORKLOAD, "N": p.N, "d": p.d, "swarm": S, "likelihood": "concentrated",
+                       "trailing_update": mode,
                        "kernel": "rbf(17) + periodic(7)", "l2": "inputs larger than L2: 40 K matrices = 5.3 GB "
                        "written per step", "parallelism": f"replicas x{ws} (independent swarms per GPU)"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,

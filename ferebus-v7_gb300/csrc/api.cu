@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -111,7 +112,25 @@ struct Workspace {
   int* status = nullptr;
   double* out = nullptr;
   double* z = nullptr;
+  // tensor-core mode
+  int* escale = nullptr;
+  double* pw2 = nullptr;
+  long long* acc_hi = nullptr;
+  long long* acc_lo = nullptr;
+  unsigned char* slices = nullptr;
 };
+
+// Process-wide default trailing-update mode for contexts created from now on:
+// 1 = tcgen05 split-integer update (128-wide panels), 0 = FP64 mma.sync.
+// The environment variable FGPU_TRAILING=fp64 selects 0 at load time.
+int g_default_mode = -1;
+int default_mode() {
+  if (g_default_mode < 0) {
+    const char* v = getenv("FGPU_TRAILING");
+    g_default_mode = (v && (strcmp(v, "fp64") == 0 || strcmp(v, "0") == 0)) ? 0 : 1;
+  }
+  return g_default_mode;
+}
 
 // Optional per-launch event pairs for stage timing (captured into the graph).
 struct StageEvents {
@@ -141,6 +160,8 @@ struct Worker {
 
 struct fgpu_ctx {
   int device = 0;
+  int mode = 1;
+  int nt128 = 0;
   int N = 0, d = 0, Nc = 0, ld = 0, nsteps = 0, nrhs = 1, likelihood = 0, optimise_noise = 0;
   int nkparams = 0, ntheta = 0;
   double noise = 0.0;
@@ -154,7 +175,7 @@ struct fgpu_ctx {
 };
 
 struct fgpu_plan {
-  int device = 0, nprob = 0, ldtheta = 0, max_nsteps = 0, max_nplanes = 0;
+  int device = 0, nprob = 0, ldtheta = 0, max_nsteps = 0, max_nplanes = 0, mode = 0;
   std::vector<fgpu_ctx*> ctxs;
   std::vector<Prob> probs_h;
   Prob* probs_d = nullptr;
@@ -198,6 +219,13 @@ void fill_prob(Prob& p, const fgpu_ctx* c, const double* theta_d, const Workspac
   p.status = ws.status;
   p.out = ws.out;
   p.z = ws.z;
+  p.mode = c->mode;
+  p.nt128 = c->nt128;
+  p.escale = ws.escale;
+  p.pw2 = ws.pw2;
+  p.acc_hi = ws.acc_hi;
+  p.acc_lo = ws.acc_lo;
+  p.slices = ws.slices;
 }
 
 int mark(StageEvents* pe, int stage, cudaStream_t s, bool begin) {
@@ -223,10 +251,28 @@ int mark(StageEvents* pe, int stage, cudaStream_t s, bool begin) {
 
 // Enqueue the whole evaluation: reset, build, sweep, epilogue.
 int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes, int* status_base,
-                 size_t status_bytes, cudaStream_t s, long long* kernels, StageEvents* pe) {
+                 size_t status_bytes, cudaStream_t s, long long* kernels, StageEvents* pe, int mode = 0) {
   long long n = 0;
   CK(cudaMemsetAsync(status_base, 0, status_bytes, s));
   STAGE(0, launch_build(probs_d, nprob, max_nsteps, max_nplanes, s));
+  if (mode == 1) {
+    // 128-wide panels; max_nsteps counts 64-column tiles
+    const int nt = max_nsteps / 2, max_nc = max_nsteps * TB;
+    STAGE(0, launch_scales(probs_d, nprob, max_nc, s));
+    for (int step = 0; step < nt; ++step) {
+      if (step > 0) STAGE(5, launch_panel_prep(probs_d, nprob, step, max_nc, s));
+      STAGE(1, launch_potf2_128(probs_d, nprob, step, s));
+      STAGE(2, launch_trsm128(probs_d, nprob, step, nt, s));
+      if (step + 1 < nt) {
+        STAGE(6, launch_split(probs_d, nprob, step, nt, s));
+        STAGE(3, launch_ozaki_update(probs_d, nprob, step, nt, s));
+        STAGE(7, launch_border_update(probs_d, nprob, step, max_nc, s));
+      }
+    }
+    STAGE(4, launch_finalize(probs_d, nprob, s));
+    if (kernels) *kernels = n;
+    return 0;
+  }
   for (int step = 0; step < max_nsteps; ++step) {
     STAGE(1, launch_potf2(probs_d, nprob, step, s));
     STAGE(2, launch_trsm(probs_d, nprob, step, max_nsteps, s));
@@ -239,9 +285,10 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
 
 int capture(cudaStream_t s, cudaGraphExec_t* exec, const Prob* probs_d, int nprob, int max_nsteps,
             int max_nplanes, int* status_base, size_t status_bytes, long long* kernels,
-            StageEvents* pe = nullptr) {
+            StageEvents* pe = nullptr, int mode = 0) {
   CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  int rc = enqueue_eval(probs_d, nprob, max_nsteps, max_nplanes, status_base, status_bytes, s, kernels, pe);
+  int rc = enqueue_eval(probs_d, nprob, max_nsteps, max_nplanes, status_base, status_bytes, s, kernels, pe,
+                        mode);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(s, &g);
   if (rc != 0) {
@@ -260,11 +307,18 @@ int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track)
   CK(cudaMalloc(&ws.logdet_part, sizeof(double) * (c->nsteps + 1)));
   CK(cudaMalloc(&ws.out, sizeof(double) * 8));
   CK(cudaMalloc(&ws.z, sizeof(double) * c->Nc));
+  if (c->mode == 1) {
+    const size_t nc = (size_t)c->Nc;
+    CK(cudaMalloc(&ws.escale, sizeof(int) * nc));
+    CK(cudaMalloc(&ws.pw2, sizeof(double) * nc));
+    CK(cudaMalloc(&ws.acc_hi, sizeof(long long) * nc * nc));
+    CK(cudaMalloc(&ws.acc_lo, sizeof(long long) * nc * nc));
+    CK(cudaMalloc(&ws.slices, (size_t)c->nt128 * NSLICE * SLICE_BYTES));
+  }
   if (track) {
-    track->push_back(ws.K);
-    track->push_back(ws.logdet_part);
-    track->push_back(ws.out);
-    track->push_back(ws.z);
+    for (void* q : {(void*)ws.K, (void*)ws.logdet_part, (void*)ws.out, (void*)ws.z, (void*)ws.escale,
+                    (void*)ws.pw2, (void*)ws.acc_hi, (void*)ws.acc_lo, (void*)ws.slices})
+      if (q) track->push_back(q);
   }
   return 0;
 }
@@ -277,6 +331,11 @@ void free_worker(Worker* w) {
   cudaFree(w->ws.status);
   cudaFree(w->ws.out);
   cudaFree(w->ws.z);
+  cudaFree(w->ws.escale);
+  cudaFree(w->ws.pw2);
+  cudaFree(w->ws.acc_hi);
+  cudaFree(w->ws.acc_lo);
+  cudaFree(w->ws.slices);
   cudaFree(w->theta_d);
   cudaFree(w->prob_d);
   if (w->h_stage) cudaFreeHost(w->h_stage);
@@ -307,7 +366,7 @@ int make_worker(fgpu_ctx* c, Worker** out) {
   if (cudaMemcpy(w->prob_d, &p, sizeof(Prob), cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(FGPU_ECUDA, "desc copy"));
   if ((rc = capture(w->stream, &w->graph, w->prob_d, 1, c->nsteps, c->spec.nplanes, w->ws.status,
-                    sizeof(int) * 4, &w->graph_kernels)) != 0)
+                    sizeof(int) * 4, &w->graph_kernels, nullptr, c->mode)) != 0)
     return bail(rc);
   *out = w;
   return 0;
@@ -367,7 +426,9 @@ int fgpu_create(fgpu_ctx** out, int N, int d, const double* X, const double* y, 
   if (rc) return rc;
   c->N = N;
   c->d = d;
-  c->Nc = round_up(N, TB);
+  c->mode = default_mode();
+  c->Nc = round_up(N, c->mode == 1 ? NB : TB);
+  c->nt128 = c->Nc / NB;
   c->ld = c->Nc + TB;
   c->nsteps = c->Nc / TB;
   c->likelihood = likelihood;
@@ -410,6 +471,13 @@ int fgpu_create(fgpu_ctx** out, int N, int d, const double* X, const double* y, 
 }
 
 int fgpu_nparams(const fgpu_ctx* ctx) { return ctx ? ctx->ntheta : FGPU_EINVAL; }
+
+int fgpu_set_trailing_update(int mode) {
+  const int prev = default_mode();
+  if (mode != 0 && mode != 1) return fail(FGPU_EINVAL, "trailing-update mode must be 0 (fp64) or 1 (tcgen05)");
+  g_default_mode = mode;
+  return prev;
+}
 
 void fgpu_destroy(fgpu_ctx* ctx) {
   if (!ctx) return;
@@ -466,7 +534,9 @@ int fgpu_loglik(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, int*
   CK(cudaMemcpyAsync(w->h_status, w->ws.status, sizeof(int) * 4, cudaMemcpyDeviceToHost, w->stream));
   if (alpha) CK(cudaMemcpyAsync(alpha, w->ws.z, sizeof(double) * ctx->N, cudaMemcpyDeviceToHost, w->stream));
   CK(cudaStreamSynchronize(w->stream));
-  if (w->h_status[2]) return fail(FGPU_ETIMEOUT, "bulk copy into shared memory did not complete");
+  if (w->h_status[2]) return fail(FGPU_ETIMEOUT, "a bounded wait in a kernel gave up (copy or MMA)");
+  if (w->h_status[3] && !w->h_status[1])
+    return fail(FGPU_ECUDA, "panel value outside its row scale bound (split-integer update)");
   *info = w->h_status[0];
   *ll = (*info == 0) ? h_out[0] : std::nan("");
   return 0;
@@ -495,6 +565,7 @@ int fgpu_plan_create(fgpu_plan** out, fgpu_ctx* const* ctxs, int nprob, int ldth
     if (!ctxs[i]) return fail(FGPU_EINVAL, "ctxs[%d] is NULL", i);
     if (ctxs[i]->device != p->device) return fail(FGPU_EINVAL, "plan spans devices");
     maxth = std::max(maxth, ctxs[i]->ntheta);
+    if (ctxs[i]->mode != ctxs[0]->mode) return fail(FGPU_EINVAL, "plan mixes trailing-update modes");
     p->max_nsteps = std::max(p->max_nsteps, ctxs[i]->nsteps);
     p->max_nplanes = std::max(p->max_nplanes, ctxs[i]->spec.nplanes);
     p->ctxs.push_back(ctxs[i]);
@@ -531,8 +602,9 @@ int fgpu_plan_create(fgpu_plan** out, fgpu_ctx* const* ctxs, int nprob, int ldth
     p->probs_h[i].info_dst = p->info_d + i;
   }
   CK(cudaMemcpy(p->probs_d, p->probs_h.data(), sizeof(Prob) * nprob, cudaMemcpyHostToDevice));
+  p->mode = ctxs[0]->mode;
   int rc = capture(p->stream, &p->graph, p->probs_d, nprob, p->max_nsteps, p->max_nplanes, p->status_all,
-                   sizeof(int) * 4 * nprob, &p->graph_kernels);
+                   sizeof(int) * 4 * nprob, &p->graph_kernels, nullptr, p->mode);
   if (rc) {
     fgpu_plan_destroy(p.release());
     return rc;
@@ -572,7 +644,7 @@ int fgpu_plan_set_profiling(fgpu_plan* p, int enable) {
   cudaGraphExec_t g = nullptr;
   long long nk = 0;
   int rc = capture(p->stream, &g, p->probs_d, p->nprob, p->max_nsteps, p->max_nplanes, p->status_all,
-                   sizeof(int) * 4 * p->nprob, &nk, p->prof);
+                   sizeof(int) * 4 * p->nprob, &nk, p->prof, p->mode);
   if (rc) return rc;
   if (p->graph) cudaGraphExecDestroy(p->graph);
   p->graph = g;
@@ -632,8 +704,10 @@ int fgpu_plan_run(fgpu_plan* p, const double* theta_host, double* ll_host, int* 
   CK(cudaStreamSynchronize(p->stream));
   memcpy(ll_host, p->h_ll, sizeof(double) * p->nprob);
   memcpy(info_host, p->h_info, sizeof(int) * p->nprob);
-  for (int i = 0; i < p->nprob; ++i)
-    if (info_host[i] < 0) return fail(FGPU_ETIMEOUT, "problem %d: bulk copy did not complete", i);
+  for (int i = 0; i < p->nprob; ++i) {
+    if (info_host[i] == -1) return fail(FGPU_ETIMEOUT, "problem %d: a bounded wait in a kernel gave up", i);
+    if (info_host[i] < 0) return fail(FGPU_ECUDA, "problem %d: panel value outside its row scale bound", i);
+  }
   return 0;
 }
 

@@ -434,9 +434,10 @@ __global__ void __launch_bounds__(256) k_finalize(const Prob* __restrict__ probs
   __shared__ double red[32];
   const int tid = threadIdx.x;
   const int N = P.N;
-  if (P.status[1] || P.status[2]) {
+  if (P.status[1] || P.status[2] || P.status[3]) {
     if (tid == 0) {
-      const int info = P.status[2] ? -1 : P.status[0];
+      // -1: a bounded wait gave up; -2: a panel value broke its row's scale bound
+      const int info = P.status[2] ? -1 : (P.status[3] && !P.status[1] ? -2 : P.status[0]);
       P.out[0] = nan("");
       P.status[0] = info;
       if (P.ll_dst) *P.ll_dst = nan("");

@@ -63,6 +63,14 @@ struct Prob {
   double* z;                      // Nc: the vector alpha's back-substitution starts from
   double* ll_dst;                 // optional extra destination for ll (batch output)
   int* info_dst;                  // optional extra destination for info
+  // tensor-core (split-integer) trailing update; unused in FP64 mode
+  int mode;                       // 0: FP64 mma.sync 64-panels, 1: tcgen05 split update, 128-panels
+  int nt128;                      // Nc / 128 (mode 1)
+  int* escale;                    // Nc: per-row power-of-two scale e_i, |L_ik| <= 2^e_i
+  double* pw2;                    // Nc: 2^(e_i - 31)
+  long long* acc_hi;              // Nc x Nc in 128 x 64 tiles: exact sums of products, high part
+  long long* acc_lo;              // low part (value = (hi * 2^32 + lo) * 2^(e_i + e_j - 62))
+  unsigned char* slices;          // nt128 x 7 x 32 KB: fp16 digit planes of the current panel
 };
 
 // Launch helpers (engine.cu).  All kernels take a device array of problems
@@ -76,6 +84,18 @@ cudaError_t launch_finalize(const Prob* probs, int nprob, cudaStream_t s);
 cudaError_t launch_backsolve(const Prob* probs, int nprob, int max_nsteps, double* alpha_out,
                              cudaStream_t s, long long* nlaunch);
 size_t build_smem_bytes(int nplanes);
+
+// Split-integer tensor-core path (ozaki.cu): 128-wide panels.
+constexpr int NB = 128;
+constexpr int NSLICE = 7;                       // fp16 digit planes per FP64 value
+constexpr size_t SLICE_BYTES = 128 * 128 * 2;   // one digit plane of a 128-row x 128-k tile
+cudaError_t launch_scales(const Prob* probs, int nprob, int max_nc, cudaStream_t s);
+cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
+cudaError_t launch_potf2_128(const Prob* probs, int nprob, int step, cudaStream_t s);
+cudaError_t launch_trsm128(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
+cudaError_t launch_split(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
+cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
+cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
 
 // api.cu hooks for other translation units.
 int internal_compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>& plane_dim,

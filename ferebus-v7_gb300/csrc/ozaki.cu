@@ -1,0 +1,544 @@
+// Tensor-core trailing update for the FP64 Cholesky (mode 1).
+//
+// GB300 executes FP64 at about 1.1 TFLOP/s, so the O(N^3) trailing update is
+// moved to the 5th-generation tensor cores as an exact integer computation
+// (the error-free splitting of Ozaki, Ogita and Oishi, "Error-free
+// transformations of matrix multiplication by using fast routines of matrix
+// multiplication and its applications", Numer. Algorithms 59, 2012, with the
+// power-of-two row scaling of its tensor-core use by Mukunoki et al., 2020):
+//
+//  * Row i of the factor has a FIXED power-of-two scale 2^e_i >= sqrt(K_ii):
+//    since sum_k L_ik^2 = K_ii, every |L_ik| <= 2^e_i for all panels.
+//  * L_ik 2^-e_i is rounded to 55 fractional bits and written as 7 signed
+//    base-256 digits d_0..d_6 (|d| <= 129), one fp16 plane per digit.
+//  * For a 128-wide panel, digit planes p (rows i) and q (rows j) are
+//    multiplied by tcgen05.mma kind::f16 with f32 accumulation.  Products
+//    are exact (|d_p d_q| < 2^15) and every partial sum of one level
+//    L = p + q (at most 7 pairs x 128 terms x 129^2 < 2^24) is an exact
+//    integer in f32, so the 7 level accumulators in TMEM hold exact integers.
+//    Levels p + q > 6 (weights below 2^-62 of the row scales) are dropped.
+//  * The epilogue turns the 7 exact level sums into two int64 words and
+//    ADDS them to per-element integer accumulators in HBM: the trailing
+//    matrix update is exact integer arithmetic, order independent, and uses
+//    no FP64 instruction.  When a block column becomes the next panel, one
+//    FP64 conversion per element subtracts the accumulated sum from K.
+//
+// The diagonal 128 x 128 factor, the panel solve and the right-hand-side
+// (border) rows stay in FP64.
+#include "fgpu_internal.h"
+
+#include <cuda_fp16.h>
+
+#include <cmath>
+
+namespace fgpu {
+
+namespace {
+
+__device__ __forceinline__ uint32_t su32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(su32(dst)),
+      "l"(src), "r"(bytes), "r"(su32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(su32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// tcgen05 shared-memory descriptor, no swizzle, K-major core matrices
+// (8 rows x 16 bytes): lbo = byte stride between core matrices along K,
+// sbo = along M/N; descriptor version 1 (bits 46-47).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+// kind::f16 instruction descriptor: f32 accumulator, f16 A/B, both K-major, M=128, N=64.
+constexpr uint32_t IDESC_128x64 = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC_128x64), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
+               : "memory");
+}
+
+// round(x * 2^(55 - e)) for |x| <= 2^e, with integer operations only.
+// Sets *bad when the scale bound is violated (|x| > 2^(e+3)).
+__device__ __forceinline__ long long to_fixed55(double x, int e, bool* bad) {
+  const long long bits = __double_as_longlong(x);
+  const int E = (int)((bits >> 52) & 0x7FF);
+  if (E == 0) return 0;  // zero or subnormal (below 2^-1022: far under the 2^-55 resolution)
+  if (E == 0x7FF) {
+    *bad = true;
+    return 0;
+  }
+  const long long M = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+  const int sh = E - 1075 + 55 - e;
+  long long F;
+  if (sh >= 0) {
+    if (sh > 3) {
+      *bad = true;
+      return 0;
+    }
+    F = M << sh;
+  } else if (sh > -63) {
+    F = (M + (1LL << (-sh - 1))) >> (-sh);
+  } else {
+    F = 0;
+  }
+  return bits < 0 ? -F : F;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// per-row scales from the diagonal of K
+// ---------------------------------------------------------------------------
+__global__ void k_scales(const Prob* __restrict__ probs) {
+  const Prob& P = probs[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (P.mode != 1 || i >= P.Nc) return;
+  const double d = P.K[(size_t)i * P.ld + i];
+  int e = 0;
+  if (d > 0.0 && d < 1e300) {
+    int E;
+    frexp(sqrt(d) * (1.0 + 0x1p-20), &E);  // sqrt(K_ii) (1 + 2^-20) < 2^E
+    e = E;
+  }
+  P.escale[i] = e;
+  P.pw2[i] = ldexp(1.0, e - 31);
+}
+
+// ---------------------------------------------------------------------------
+// block column s: K_ij -= (hi 2^32 + lo) 2^(e_i + e_j - 62), rows [c0, Nc)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ probs, int s) {
+  const Prob& P = probs[blockIdx.z];
+  if (P.mode != 1 || s >= P.nt128 || s == 0 || P.status[1]) return;
+  const int c0 = s * NB;
+  const int i = c0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.Nc) return;
+  const size_t ld = (size_t)P.ld;
+  const double pi = P.pw2[i];
+  for (int jj = 0; jj < 16; ++jj) {
+    const int j = c0 + blockIdx.y * 16 + jj;
+    const size_t a = ((size_t)((j >> 6) * P.nt128 + (i >> 7)) * 64 + (j & 63)) * 128 + (i & 127);
+    const double w = fma((double)P.acc_hi[a], 4294967296.0, (double)P.acc_lo[a]);
+    double* kp = P.K + (size_t)j * ld + i;
+    *kp = *kp - w * pi * P.pw2[j];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 128 x 128 diagonal block factorisation (FP64) + log-det partial
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) k_potf2_128(const Prob* __restrict__ probs, int s) {
+  const Prob& P = probs[blockIdx.x];
+  if (P.mode != 1 || s >= P.nt128 || P.status[1]) return;
+  extern __shared__ __align__(16) double A[];  // 128 x 129
+  __shared__ double rdiag;
+  __shared__ int fail_col;
+  __shared__ double red[16];
+  constexpr int S = NB + 1;
+  const int tid = threadIdx.x;
+  const size_t ld = (size_t)P.ld;
+  double* Kd = P.K + (size_t)(s * NB) * ld + s * NB;
+  for (int e = tid; e < NB * NB; e += blockDim.x) {
+    const int r = e % NB, c = e / NB;
+    A[c * S + r] = Kd[(size_t)c * ld + r];
+  }
+  if (tid == 0) fail_col = -1;
+  __syncthreads();
+  for (int j = 0; j < NB; ++j) {
+    if (tid == 0) {
+      const double d = A[j * S + j];
+      if (!(d > 0.0)) {
+        fail_col = j;
+      } else {
+        const double sq = sqrt(d);
+        A[j * S + j] = sq;
+        rdiag = 1.0 / sq;
+      }
+    }
+    __syncthreads();
+    if (fail_col >= 0) break;
+    if (tid > j && tid < NB) A[j * S + tid] *= rdiag;
+    __syncthreads();
+    const int w = NB - 1 - j;
+    for (int e = tid; e < w * w; e += blockDim.x) {
+      const int r = j + 1 + e % w, c = j + 1 + e / w;
+      if (r >= c) A[c * S + r] = fma(-A[j * S + r], A[j * S + c], A[c * S + r]);
+    }
+    __syncthreads();
+  }
+  if (fail_col >= 0) {
+    if (tid == 0) {
+      P.status[0] = s * NB + fail_col + 1;
+      P.status[1] = 1;
+    }
+    return;
+  }
+  for (int e = tid; e < NB * NB; e += blockDim.x) {
+    const int r = e % NB, c = e / NB;
+    if (r >= c) Kd[(size_t)c * ld + r] = A[c * S + r];
+  }
+  // log-det partial in the slots of the two 64-column halves
+  double v = tid < NB ? log(A[tid * S + tid]) : 0.0;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 4; ++w) t += red[w];
+    P.logdet_part[2 * s] = t;
+    P.logdet_part[2 * s + 1] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// panel solve with the 128-wide L11 (FP64), 64-row tiles incl. the border tile
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_trsm128(const Prob* __restrict__ probs, int s) {
+  const Prob& P = probs[blockIdx.y];
+  const int ti = 2 * (s + 1) + blockIdx.x;  // 64-row tile index; P.nsteps is the border tile
+  if (P.mode != 1 || s >= P.nt128 || ti > P.nsteps || P.status[1]) return;
+  extern __shared__ __align__(16) double smd[];
+  constexpr int S = NB + 1;   // L11: 128 x 128, column stride 129
+  constexpr int SB = TB + 1;  // panel rows: 64 x 128, column stride 65
+  double* L = smd;
+  double* B = smd + NB * S;
+  double* rd = B + NB * SB;
+  const int tid = threadIdx.x;
+  const size_t ld = (size_t)P.ld;
+  const double* Ld = P.K + (size_t)(s * NB) * ld + s * NB;
+  double* Bd = P.K + (size_t)(s * NB) * ld + ti * TB;
+  for (int e = tid; e < NB * NB; e += blockDim.x) {
+    const int r = e % NB, c = e / NB;
+    L[c * S + r] = Ld[(size_t)c * ld + r];
+  }
+  for (int e = tid; e < TB * NB; e += blockDim.x) {
+    const int r = e % TB, c = e / TB;
+    B[c * SB + r] = Bd[(size_t)c * ld + r];
+  }
+  __syncthreads();
+  if (tid < NB) rd[tid] = 1.0 / L[tid * S + tid];
+  __syncthreads();
+  for (int c = 0; c < NB; ++c) {
+    if (tid < TB) B[c * SB + tid] *= rd[c];
+    __syncthreads();
+    const int w = NB - 1 - c;
+    for (int e = tid; e < w * TB; e += blockDim.x) {
+      const int r = e % TB, q = c + 1 + e / TB;
+      B[q * SB + r] = fma(-B[c * SB + r], L[c * S + q], B[q * SB + r]);
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < TB * NB; e += blockDim.x) {
+    const int r = e % TB, c = e / TB;
+    Bd[(size_t)c * ld + r] = B[c * SB + r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// digit planes of the panel rows below the diagonal block
+// layout per 128-row tile and digit p: [kgroup 16][row 128][8 k] fp16
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, int s) {
+  const Prob& P = probs[blockIdx.z];
+  const int ti = s + 1 + blockIdx.x;
+  if (P.mode != 1 || ti >= P.nt128 || P.status[1]) return;
+  const int r = threadIdx.x, kg = blockIdx.y;
+  const int i = ti * NB + r;
+  const int e = P.escale[i];
+  const size_t ld = (size_t)P.ld;
+  const double* col = P.K + (size_t)(s * NB + kg * 8) * ld + i;
+  int d[NSLICE][8];
+  bool bad = false;
+  for (int kk = 0; kk < 8; ++kk) {
+    long long F = to_fixed55(col[(size_t)kk * ld], e, &bad);
+    for (int p = NSLICE - 1; p >= 1; --p) {
+      const int b = (int)(signed char)(F & 0xFF);
+      d[p][kk] = b;
+      F = (F - b) >> 8;
+    }
+    d[0][kk] = (int)F;
+  }
+  if (bad) atomicOr(&P.status[3], 1);
+  unsigned char* base = P.slices + (size_t)ti * NSLICE * SLICE_BYTES + (size_t)kg * 2048 + (size_t)r * 16;
+  for (int p = 0; p < NSLICE; ++p) {
+    __align__(16) __half h[8];
+    for (int kk = 0; kk < 8; ++kk) h[kk] = __int2half_rn(d[p][kk]);
+    *reinterpret_cast<uint4*>(base + (size_t)p * SLICE_BYTES) = *reinterpret_cast<const uint4*>(h);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// trailing update of the integer accumulators for one 128 x 64 output tile
+//
+// Accumulators are stored tile-major (128 x 64 tiles, column-major inside),
+// so one tile of each word is a contiguous 64 KB block: it is prefetched into
+// shared memory by the bulk-copy engine while the MMAs run, and the epilogue
+// adds to it without waiting on HBM.
+// ---------------------------------------------------------------------------
+constexpr int CH = 8;                                // k-chunks of 16 per 128-panel (one MMA each)
+constexpr uint32_t A_STAGE = NSLICE * 4096;          // 7 planes x 128 rows x 16 k x 2 B
+constexpr uint32_t B_STAGE = NSLICE * 2048;          // 7 planes x 64 rows x 16 k x 2 B
+constexpr uint32_t STAGE = A_STAGE + B_STAGE;        // 43008 B
+constexpr uint32_t ACC_TILE = 128 * 64 * 8;          // one int64 word of a tile: 64 KB
+constexpr uint32_t UPD_SMEM = 2 * STAGE + 2 * ACC_TILE + 128;
+
+__device__ __forceinline__ size_t acc_index(int i, int j, int nt) {
+  return ((size_t)((j >> 6) * nt + (i >> 7)) * 64 + (j & 63)) * 128 + (i & 127);
+}
+
+__global__ void __launch_bounds__(256, 1) k_ozaki_update(const Prob* __restrict__ probs, int s) {
+  const Prob& P = probs[blockIdx.z];
+  if (P.mode != 1 || P.status[1]) return;
+  const int m = P.nt128 - s - 1;
+  if ((int)blockIdx.x >= m || (int)blockIdx.y >= 2 * m) return;
+  const int ti = s + 1 + blockIdx.x;            // 128-row tile
+  const int tj = 2 * (s + 1) + blockIdx.y;      // 64-column tile
+  if (tj / 2 > ti) return;                      // strictly upper
+  extern __shared__ __align__(1024) unsigned char smu[];
+  long long* acc_hi_s = reinterpret_cast<long long*>(smu + 2 * STAGE);
+  long long* acc_lo_s = reinterpret_cast<long long*>(smu + 2 * STAGE + ACC_TILE);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smu + 2 * STAGE + 2 * ACC_TILE);
+  uint64_t* empty = full + 2;
+  uint64_t* done = full + 4;
+  uint64_t* accbar = full + 5;
+  uint32_t* slot = reinterpret_cast<uint32_t*>(full + 6);
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const bool first = (s == 0);
+  const size_t tile_off = (size_t)(tj * P.nt128 + ti) * (128 * 64);
+  if (tid == 0) {
+    s_abort = 0;
+    for (int k = 0; k < 2; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], 1);
+    }
+    mbar_init(done, 1);
+    mbar_init(accbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tbase = *slot;
+
+  const unsigned char* Ag = P.slices + (size_t)ti * NSLICE * SLICE_BYTES;
+  const unsigned char* Bg = P.slices + (size_t)(tj / 2) * NSLICE * SLICE_BYTES + (size_t)(tj % 2) * 1024;
+
+  if (tid == 0) {
+    if (!first) {
+      mbar_expect_tx(accbar, 2 * ACC_TILE);
+      bulk_g2s(acc_hi_s, P.acc_hi + tile_off, ACC_TILE, accbar);
+      bulk_g2s(acc_lo_s, P.acc_lo + tile_off, ACC_TILE, accbar);
+    }
+    auto load = [&](int c, int st) {
+      unsigned char* As = smu + st * STAGE;
+      unsigned char* Bs = As + A_STAGE;
+      mbar_expect_tx(&full[st], STAGE);
+      for (int p = 0; p < NSLICE; ++p) {
+        bulk_g2s(As + p * 4096, Ag + (size_t)p * SLICE_BYTES + (size_t)c * 4096, 4096, &full[st]);
+        for (int kq = 0; kq < 2; ++kq)
+          bulk_g2s(Bs + p * 2048 + kq * 1024, Bg + (size_t)p * SLICE_BYTES + (size_t)(2 * c + kq) * 2048, 1024,
+                   &full[st]);
+      }
+    };
+    load(0, 0);
+    load(1, 1);
+    bool ok = true;
+    for (int c = 0; c < CH && ok; ++c) {
+      const int st = c & 1;
+      ok = mbar_wait(&full[st], (c >> 1) & 1);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t As = su32(smu + st * STAGE);
+      const uint32_t Bs = As + A_STAGE;
+      for (int p = 0; p < NSLICE; ++p) {
+        const uint64_t ad = smem_desc(As + p * 4096, 2048, 128);
+        for (int q = 0; q + p < NSLICE; ++q) {
+          const uint64_t bd = smem_desc(Bs + q * 2048, 1024, 128);
+          mma_f16(tbase + (uint32_t)(p + q) * 64, ad, bd, (c == 0 && p == 0) ? 0u : 1u);
+        }
+      }
+      mma_commit(&empty[st]);
+      if (c >= 1 && c + 1 < CH) {
+        const int pst = (c - 1) & 1;
+        ok = mbar_wait(&empty[pst], ((c - 1) >> 1) & 1);
+        if (ok) load(c + 1, pst);
+      }
+    }
+    mma_commit(done);
+    if (!ok) s_abort = 1;
+  }
+  bool fin = mbar_wait(done, 0);
+  if (!first) fin = fin && mbar_wait(accbar, 0);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (!fin || s_abort) {
+    if (tid == 0) atomicExch(&P.status[2], 1);
+  } else {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its rows) and the
+    // column half w / 4; 7 exact level sums -> two int64 words per element
+    const int r = (warp & 3) * 32 + (tid & 31);
+    const int h = warp >> 2;
+    long long* gh = P.acc_hi + tile_off;
+    long long* gl = P.acc_lo + tile_off;
+    for (int cc = 0; cc < 4; ++cc) {
+      const int col0 = h * 32 + cc * 8;
+      uint32_t v[NSLICE][8];
+      for (int l = 0; l < NSLICE; ++l) {
+        const uint32_t ta = tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(l * 64 + col0);
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]), "=r"(v[l][5]),
+                       "=r"(v[l][6]), "=r"(v[l][7])
+                     : "r"(ta));
+      }
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      for (int jj = 0; jj < 8; ++jj) {
+        long long S[NSLICE];
+        for (int l = 0; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
+        long long hi = S[0] * 65536 + S[1] * 256 + S[2];
+        long long lo = S[3] * 16777216 + S[4] * 65536 + S[5] * 256 + S[6];
+        const int idx = (col0 + jj) * 128 + r;
+        if (!first) {
+          hi += acc_hi_s[idx];
+          lo += acc_lo_s[idx];
+        }
+        gh[idx] = hi;
+        gl[idx] = lo;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
+}
+
+// ---------------------------------------------------------------------------
+// right-hand-side rows: C_qj -= sum_k Z_qk L_jk over the panel (FP64)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_border_update(const Prob* __restrict__ probs, int s) {
+  const Prob& P = probs[blockIdx.y];
+  if (P.mode != 1 || s + 1 >= P.nt128 || P.status[1]) return;
+  __shared__ double Z[MAX_RHS][NB];
+  const size_t ld = (size_t)P.ld;
+  const int c0 = s * NB;
+  for (int e = threadIdx.x; e < MAX_RHS * NB; e += blockDim.x) {
+    const int q = e / NB, k = e % NB;
+    Z[q][k] = q < P.nrhs ? P.K[(size_t)(c0 + k) * ld + P.Nc + q] : 0.0;
+  }
+  __syncthreads();
+  const int j = c0 + NB + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= P.Nc) return;
+  double a0 = 0.0, a1 = 0.0;
+  for (int k = 0; k < NB; ++k) {
+    const double l = P.K[(size_t)(c0 + k) * ld + j];
+    a0 = fma(Z[0][k], l, a0);
+    a1 = fma(Z[1][k], l, a1);
+  }
+  P.K[(size_t)j * ld + P.Nc] -= a0;
+  if (P.nrhs > 1) P.K[(size_t)j * ld + P.Nc + 1] -= a1;
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+static bool g_attr = false;
+constexpr int TRSM128_SMEM = (NB * (NB + 1) + NB * (TB + 1) + NB) * (int)sizeof(double);
+static cudaError_t set_attrs() {
+  if (g_attr) return cudaSuccess;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_potf2_128, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                NB * (NB + 1) * (int)sizeof(double))) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_trsm128, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                TRSM128_SMEM)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_ozaki_update, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM)) !=
+      cudaSuccess)
+    return e;
+  g_attr = true;
+  return cudaSuccess;
+}
+
+cudaError_t launch_scales(const Prob* probs, int nprob, int max_nc, cudaStream_t s) {
+  k_scales<<<dim3((max_nc + 255) / 256, nprob), 256, 0, s>>>(probs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s) {
+  const int rows = max_nc - step * NB;
+  if (step == 0 || rows <= 0) return cudaSuccess;
+  k_panel_prep<<<dim3((rows + 255) / 256, NB / 16, nprob), 256, 0, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_potf2_128(const Prob* probs, int nprob, int step, cudaStream_t s) {
+  cudaError_t e = set_attrs();
+  if (e != cudaSuccess) return e;
+  k_potf2_128<<<nprob, 512, NB * (NB + 1) * sizeof(double), s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trsm128(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
+  cudaError_t e = set_attrs();
+  if (e != cudaSuccess) return e;
+  const int tiles = 2 * max_nt128 + 1 - 2 * (step + 1);  // 64-row tiles below the block, incl. border
+  if (tiles <= 0) return cudaSuccess;
+  k_trsm128<<<dim3(tiles, nprob), 256, TRSM128_SMEM, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
+  const int m = max_nt128 - step - 1;
+  if (m <= 0) return cudaSuccess;
+  k_split<<<dim3(m, NB / 8, nprob), 128, 0, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
+  cudaError_t e = set_attrs();
+  if (e != cudaSuccess) return e;
+  const int m = max_nt128 - step - 1;
+  if (m <= 0) return cudaSuccess;
+  k_ozaki_update<<<dim3(m, 2 * m, nprob), 256, UPD_SMEM, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s) {
+  const int cols = max_nc - (step + 1) * NB;
+  if (cols <= 0) return cudaSuccess;
+  k_border_update<<<dim3((cols + 255) / 256, nprob), 256, 0, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+}  // namespace fgpu

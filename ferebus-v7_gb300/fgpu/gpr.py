@@ -123,12 +123,12 @@ class Plan:
     def set_profiling(self, enable=True):
         _lib.check(self.lib.fgpu_plan_set_profiling(self.handle, 1 if enable else 0))
 
-    STAGES = ("build", "potf2", "trsm", "update", "finalize")
+    STAGES = ("build", "potf2", "trsm", "update", "finalize", "panel_prep", "split", "border")
 
     def stage_times(self):
         """{stage: (ms during the last replay, launches)}."""
-        ms = np.zeros(5)
-        cnt = np.zeros(5, dtype=np.int32)
+        ms = np.zeros(8)
+        cnt = np.zeros(8, dtype=np.int32)
         _lib.check(self.lib.fgpu_plan_stage_times(self.handle, _dp(ms), cnt.ctypes.data_as(_lib.c_int_p)))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.STAGES)}
 
@@ -142,6 +142,16 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def set_trailing_update(mode):
+    """Trailing-update arithmetic for engines created afterwards: "tcgen05"
+    (default, exact split-integer products on the tensor cores) or "fp64".
+    Returns the previous mode name."""
+    lib = _lib.load()
+    code = {"fp64": 0, "tcgen05": 1}[mode]
+    prev = _lib.check(lib.fgpu_set_trailing_update(code))
+    return {0: "fp64", 1: "tcgen05"}[prev]
 
 
 def loglik_batch(engines, thetas):

@@ -70,6 +70,19 @@ int fgpu_create(fgpu_ctx** ctx, int N, int d, const double* X, const double* y,
 /* Number of entries theta must hold (GaussianProcessRegressor%nparams, gpr.f90:248-256). */
 int fgpu_nparams(const fgpu_ctx* ctx);
 
+/* Trailing-update arithmetic of the Cholesky for contexts created after the
+ * call (process-wide default; returns the previous setting):
+ *   FGPU_TRAILING_TCGEN05 (default): 128-wide panels; the O(N^3) update runs
+ *     on the tensor cores as exact integer products of 7 fp16 digit planes
+ *     per FP64 value, accumulated exactly in int64;
+ *   FGPU_TRAILING_FP64: 64-wide panels, FP64 mma.sync on the FP64 pipe.
+ * Diagonal blocks, panel solves and the right-hand-side rows are FP64 in
+ * both.  The environment variable FGPU_TRAILING=fp64 selects FP64 at load.
+ * No counterpart in the reference (which calls LAPACK dpotrf). */
+#define FGPU_TRAILING_FP64 0
+#define FGPU_TRAILING_TCGEN05 1
+int fgpu_set_trailing_update(int mode);
+
 /* Plain drop-in: one particle per call.  Replaces
  * GaussianProcessRegressor%log_likelihood (src/model/gpr/gpr.f90:291-307) ->
  * compute_R (gpr.f90:185-189) + Likelihood%ll (src/model/gpr/likelihood.f90:161-253).
@@ -138,8 +151,9 @@ int fgpu_loglik_noalloc(int N, int d, const double* X_dev, const double* y_dev, 
  * fgpu_plan_stage_times fills ms[k] with the summed device time of stage k
  * during the LAST replay and count[k] with its launches (k: 0 build,
  * 1 diagonal factor, 2 panel solve, 3 trailing update, 4 likelihood
- * epilogue).  Diagnostic only; the reference has no counterpart. */
-#define FGPU_NSTAGES 5
+ * epilogue, 5 panel conversion, 6 digit split, 7 right-hand-side rows).
+ * Diagnostic only; the reference has no counterpart. */
+#define FGPU_NSTAGES 8
 int fgpu_plan_set_profiling(fgpu_plan* plan, int enable);
 int fgpu_plan_stage_times(fgpu_plan* plan, double* ms, int* count);
 

@@ -187,3 +187,40 @@ def test_full_size_glycine_like_config(lib):
                           tens=O.Tensors(p.X, lazy=True))
     assert rinfo == info[0] == 0
     assert abs(ll[0] - ref) <= 1e-9 * abs(ref)
+
+
+@pytest.fixture(params=["fp64", "tcgen05"])
+def trailing(request, lib):
+    from fgpu.gpr import set_trailing_update
+    prev = set_trailing_update(request.param)
+    yield request.param
+    set_trailing_update(prev)
+
+
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 255, 256, 257, 700])
+@pytest.mark.parametrize("lik", [0, 1])
+def test_both_trailing_modes_against_oracle(n, lik, trailing):
+    """The FP64 (mma.sync) and tensor-core (split-integer tcgen05) trailing
+    updates, across the 64 / 128 panel boundaries."""
+    from fgpu import Engine
+    X, y, mu, ks, th = _random_problem(n, 5, lik, seed=1000 + n + lik)
+    noise = 1e-6
+    e = Engine(X, y, mu, ks, lik, noise, False)
+    ll, info = e.loglik(th)
+    ref, rinfo = O.loglik(ks, th, X, y, mu, lik, noise, False)
+    assert info == rinfo == 0
+    if n == 1 and lik == 1:
+        assert ll > 30 and ref > 30
+    else:
+        assert abs(ll - ref) <= 1e-9 * abs(ref) + 1e-12, (trailing, ll, ref)
+
+
+@pytest.mark.parametrize("name", ["water_O1_rbf_x_per", "syn_c1_water_like", "nma_C1_rbf_conc",
+                                  "syn_c2_methanol_like", "syn_c5_noise_quadratic"])
+def test_golden_cases_in_both_modes(name, trailing):
+    c = load_case(name)
+    e = engine_for(c)
+    for k, th in enumerate(c["thetas"]):
+        ll, info = e.loglik(th)
+        assert info == int(c["info"][k]) == 0
+        assert abs(ll - c["ll"][k]) <= tol(c["ll"][k], c["spread"][k]), (trailing, k, ll, c["ll"][k])
