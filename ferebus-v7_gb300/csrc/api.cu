@@ -106,6 +106,15 @@ int compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>
   return 0;
 }
 
+// Per-step tile tables of the persistent tensor-core update: for step s,
+// prefix[s * (nprob + 1) + p] = tiles of problems < p.
+struct UpdSched {
+  int* prefix_dev = nullptr;
+  std::vector<int> totals;  // tiles per step
+  int stride = 0;           // nprob + 1
+  int num_sms = 0;
+};
+
 struct Workspace {
   double* K = nullptr;
   double* logdet_part = nullptr;
@@ -116,8 +125,9 @@ struct Workspace {
   int* escale = nullptr;
   double* pw2 = nullptr;
   long long* acc_hi = nullptr;
-  long long* acc_lo = nullptr;
+  int* acc_lo = nullptr;
   unsigned char* slices = nullptr;
+  unsigned char* tmaps = nullptr;  // 2 x 128 B TMA tensor maps over slices
 };
 
 // Process-wide default trailing-update mode for contexts created from now on:
@@ -156,6 +166,7 @@ struct Worker {
   cudaGraphExec_t graph = nullptr;
   long long graph_kernels = 0;
   bool busy = false;
+  UpdSched sched;
 };
 
 struct fgpu_ctx {
@@ -191,6 +202,7 @@ struct fgpu_plan {
   double* h_ll = nullptr;
   int* h_info = nullptr;
   StageEvents* prof = nullptr;
+  UpdSched sched;
   std::mutex mu;
 };
 
@@ -226,6 +238,34 @@ void fill_prob(Prob& p, const fgpu_ctx* c, const double* theta_d, const Workspac
   p.acc_hi = ws.acc_hi;
   p.acc_lo = ws.acc_lo;
   p.slices = ws.slices;
+  p.tmap_a = ws.tmaps;
+  p.tmap_b = ws.tmaps ? ws.tmaps + 128 : nullptr;
+}
+
+int build_sched(const std::vector<int>& nt128, UpdSched& u, std::vector<void*>* track) {
+  const int nprob = (int)nt128.size();
+  int ntmax = 0;
+  for (int v : nt128) ntmax = std::max(ntmax, v);
+  u.stride = nprob + 1;
+  std::vector<int> h((size_t)std::max(ntmax, 1) * u.stride, 0);
+  u.totals.assign(std::max(ntmax, 1), 0);
+  for (int st = 0; st < ntmax; ++st) {
+    int acc = 0;
+    for (int p = 0; p < nprob; ++p) {
+      h[(size_t)st * u.stride + p] = acc;
+      const int m = nt128[p] - st - 1;
+      if (m > 0) acc += m * (m + 1);
+    }
+    h[(size_t)st * u.stride + nprob] = acc;
+    u.totals[st] = acc;
+  }
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&u.num_sms, cudaDevAttrMultiProcessorCount, dev));
+  CK(cudaMalloc(&u.prefix_dev, sizeof(int) * h.size()));
+  if (track) track->push_back(u.prefix_dev);
+  CK(cudaMemcpy(u.prefix_dev, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
+  return 0;
 }
 
 int mark(StageEvents* pe, int stage, cudaStream_t s, bool begin) {
@@ -251,7 +291,8 @@ int mark(StageEvents* pe, int stage, cudaStream_t s, bool begin) {
 
 // Enqueue the whole evaluation: reset, build, sweep, epilogue.
 int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes, int* status_base,
-                 size_t status_bytes, cudaStream_t s, long long* kernels, StageEvents* pe, int mode = 0) {
+                 size_t status_bytes, cudaStream_t s, long long* kernels, StageEvents* pe, int mode = 0,
+                 const UpdSched* us = nullptr) {
   long long n = 0;
   CK(cudaMemsetAsync(status_base, 0, status_bytes, s));
   STAGE(0, launch_build(probs_d, nprob, max_nsteps, max_nplanes, s));
@@ -265,7 +306,8 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
       STAGE(2, launch_trsm128(probs_d, nprob, step, nt, s));
       if (step + 1 < nt) {
         STAGE(6, launch_split(probs_d, nprob, step, nt, s));
-        STAGE(3, launch_ozaki_update(probs_d, nprob, step, nt, s));
+        STAGE(3, launch_ozaki_update(probs_d, nprob, step, nt, us->prefix_dev + (size_t)step * us->stride,
+                                     us->totals[step], us->num_sms, s));
         STAGE(7, launch_border_update(probs_d, nprob, step, max_nc, s));
       }
     }
@@ -285,10 +327,11 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
 
 int capture(cudaStream_t s, cudaGraphExec_t* exec, const Prob* probs_d, int nprob, int max_nsteps,
             int max_nplanes, int* status_base, size_t status_bytes, long long* kernels,
-            StageEvents* pe = nullptr, int mode = 0) {
+            StageEvents* pe = nullptr, int mode = 0, const UpdSched* us = nullptr) {
+  if (mode == 1 && !us) return fail(FGPU_EINVAL, "internal: tensor-core mode without a tile schedule");
   CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   int rc = enqueue_eval(probs_d, nprob, max_nsteps, max_nplanes, status_base, status_bytes, s, kernels, pe,
-                        mode);
+                        mode, us);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(s, &g);
   if (rc != 0) {
@@ -312,12 +355,17 @@ int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track)
     CK(cudaMalloc(&ws.escale, sizeof(int) * nc));
     CK(cudaMalloc(&ws.pw2, sizeof(double) * nc));
     CK(cudaMalloc(&ws.acc_hi, sizeof(long long) * nc * nc));
-    CK(cudaMalloc(&ws.acc_lo, sizeof(long long) * nc * nc));
+    CK(cudaMalloc(&ws.acc_lo, sizeof(int) * nc * nc));
     CK(cudaMalloc(&ws.slices, (size_t)c->nt128 * NSLICE * SLICE_BYTES));
+    CK(cudaMalloc(&ws.tmaps, 256));
+    alignas(64) unsigned char maps[256];
+    const int er = encode_slice_maps(maps, ws.slices, c->nt128);
+    if (er != 0) return fail(FGPU_ECUDA, "cuTensorMapEncodeTiled failed (%d)", er);
+    CK(cudaMemcpy(ws.tmaps, maps, 256, cudaMemcpyHostToDevice));
   }
   if (track) {
     for (void* q : {(void*)ws.K, (void*)ws.logdet_part, (void*)ws.out, (void*)ws.z, (void*)ws.escale,
-                    (void*)ws.pw2, (void*)ws.acc_hi, (void*)ws.acc_lo, (void*)ws.slices})
+                    (void*)ws.pw2, (void*)ws.acc_hi, (void*)ws.acc_lo, (void*)ws.slices, (void*)ws.tmaps})
       if (q) track->push_back(q);
   }
   return 0;
@@ -336,8 +384,10 @@ void free_worker(Worker* w) {
   cudaFree(w->ws.acc_hi);
   cudaFree(w->ws.acc_lo);
   cudaFree(w->ws.slices);
+  cudaFree(w->ws.tmaps);
   cudaFree(w->theta_d);
   cudaFree(w->prob_d);
+  cudaFree(w->sched.prefix_dev);
   if (w->h_stage) cudaFreeHost(w->h_stage);
   if (w->stream) cudaStreamDestroy(w->stream);
   delete w;
@@ -365,8 +415,9 @@ int make_worker(fgpu_ctx* c, Worker** out) {
   fill_prob(p, c, w->theta_d, w->ws);
   if (cudaMemcpy(w->prob_d, &p, sizeof(Prob), cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(FGPU_ECUDA, "desc copy"));
+  if (c->mode == 1 && (rc = build_sched(std::vector<int>{c->nt128}, w->sched, nullptr)) != 0) return bail(rc);
   if ((rc = capture(w->stream, &w->graph, w->prob_d, 1, c->nsteps, c->spec.nplanes, w->ws.status,
-                    sizeof(int) * 4, &w->graph_kernels, nullptr, c->mode)) != 0)
+                    sizeof(int) * 4, &w->graph_kernels, nullptr, c->mode, &w->sched)) != 0)
     return bail(rc);
   *out = w;
   return 0;
@@ -603,8 +654,17 @@ int fgpu_plan_create(fgpu_plan** out, fgpu_ctx* const* ctxs, int nprob, int ldth
   }
   CK(cudaMemcpy(p->probs_d, p->probs_h.data(), sizeof(Prob) * nprob, cudaMemcpyHostToDevice));
   p->mode = ctxs[0]->mode;
+  if (p->mode == 1) {
+    std::vector<int> nts;
+    for (int i = 0; i < nprob; ++i) nts.push_back(ctxs[i]->nt128);
+    int rs = build_sched(nts, p->sched, &p->allocations);
+    if (rs) {
+      fgpu_plan_destroy(p.release());
+      return rs;
+    }
+  }
   int rc = capture(p->stream, &p->graph, p->probs_d, nprob, p->max_nsteps, p->max_nplanes, p->status_all,
-                   sizeof(int) * 4 * nprob, &p->graph_kernels, nullptr, p->mode);
+                   sizeof(int) * 4 * nprob, &p->graph_kernels, nullptr, p->mode, &p->sched);
   if (rc) {
     fgpu_plan_destroy(p.release());
     return rc;
@@ -644,7 +704,7 @@ int fgpu_plan_set_profiling(fgpu_plan* p, int enable) {
   cudaGraphExec_t g = nullptr;
   long long nk = 0;
   int rc = capture(p->stream, &g, p->probs_d, p->nprob, p->max_nsteps, p->max_nplanes, p->status_all,
-                   sizeof(int) * 4 * p->nprob, &nk, p->prof, p->mode);
+                   sizeof(int) * 4 * p->nprob, &nk, p->prof, p->mode, &p->sched);
   if (rc) return rc;
   if (p->graph) cudaGraphExecDestroy(p->graph);
   p->graph = g;

@@ -277,10 +277,14 @@ __global__ void __launch_bounds__(256) k_potf2(const Prob* __restrict__ probs, i
     if (fail_col >= 0) break;
     if (tid > j && tid < TB) A[j * (TB + 1) + tid] *= rdiag;
     __syncthreads();
-    const int w = TB - 1 - j;  // trailing order
-    for (int e = tid; e < w * w; e += blockDim.x) {
-      const int r = j + 1 + e % w, c = j + 1 + e / w;
-      if (r >= c) A[c * (TB + 1) + r] = fma(-A[j * (TB + 1) + r], A[j * (TB + 1) + c], A[c * (TB + 1) + r]);
+    // rank-1 update: thread (row r, group g) updates columns j+1+g, +4, ... <= r
+    {
+      const int r = tid & (TB - 1), g = tid >> 6;
+      if (r > j) {
+        const double ljr = A[j * (TB + 1) + r];
+        for (int c = j + 1 + g; c <= r; c += 4)
+          A[c * (TB + 1) + r] = fma(-ljr, A[j * (TB + 1) + c], A[c * (TB + 1) + r]);
+      }
     }
     __syncthreads();
   }

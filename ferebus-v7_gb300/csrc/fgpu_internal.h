@@ -69,9 +69,15 @@ struct Prob {
   int* escale;                    // Nc: per-row power-of-two scale e_i, |L_ik| <= 2^e_i
   double* pw2;                    // Nc: 2^(e_i - 31)
   long long* acc_hi;              // Nc x Nc in 128 x 64 tiles: exact sums of products, high part
-  long long* acc_lo;              // low part (value = (hi * 2^32 + lo) * 2^(e_i + e_j - 62))
+  int* acc_lo;                    // low 24 bits (value = (hi * 2^24 + lo) * 2^(e_i + e_j - 62))
   unsigned char* slices;          // nt128 x 7 x 32 KB: fp16 digit planes of the current panel
+  const void* tmap_a;             // TMA tensor map over slices, box 8 x 128 rows x 2 kgroups x 7 planes
+  const void* tmap_b;             // same, box of 64 rows
 };
+
+// Encode the two 5-D TMA tensor maps of a problem's digit-plane buffer into
+// host memory (2 x 128 bytes).  Returns 0 or a CUDA driver error code.
+int encode_slice_maps(void* host_maps, const void* slices, int nt128);
 
 // Launch helpers (engine.cu).  All kernels take a device array of problems
 // and index it by blockIdx.y; problems whose geometry does not reach the
@@ -94,7 +100,10 @@ cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc
 cudaError_t launch_potf2_128(const Prob* probs, int nprob, int step, cudaStream_t s);
 cudaError_t launch_trsm128(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
 cudaError_t launch_split(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
-cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
+// prefix: device table of nprob + 1 tile offsets for this step (tiles of
+// problem p at step s: m (m + 1), m = nt128_p - s - 1); total_tiles = prefix[nprob].
+cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, const int* prefix,
+                                int total_tiles, int num_sms, cudaStream_t s);
 cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
 
 // api.cu hooks for other translation units.

@@ -27,9 +27,12 @@
 // (border) rows stay in FP64.
 #include "fgpu_internal.h"
 
+#include <cuda.h>
 #include <cuda_fp16.h>
+#include <cudaTypedefs.h>
 
 #include <cmath>
+#include <mutex>
 
 namespace fgpu {
 
@@ -43,12 +46,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(su32(dst)),
-      "l"(src), "r"(bytes), "r"(su32(bar))
-      : "memory");
 }
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   for (int it = 0; it < (1 << 22); ++it) {
@@ -132,7 +129,7 @@ __global__ void k_scales(const Prob* __restrict__ probs) {
 }
 
 // ---------------------------------------------------------------------------
-// block column s: K_ij -= (hi 2^32 + lo) 2^(e_i + e_j - 62), rows [c0, Nc)
+// block column s: K_ij -= (hi 2^24 + lo) 2^(e_i + e_j - 62), rows [c0, Nc)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ probs, int s) {
   const Prob& P = probs[blockIdx.z];
@@ -145,7 +142,7 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
   for (int jj = 0; jj < 16; ++jj) {
     const int j = c0 + blockIdx.y * 16 + jj;
     const size_t a = ((size_t)((j >> 6) * P.nt128 + (i >> 7)) * 64 + (j & 63)) * 128 + (i & 127);
-    const double w = fma((double)P.acc_hi[a], 4294967296.0, (double)P.acc_lo[a]);
+    const double w = fma((double)P.acc_hi[a], 16777216.0, (double)P.acc_lo[a]);
     double* kp = P.K + (size_t)j * ld + i;
     *kp = *kp - w * pi * P.pw2[j];
   }
@@ -186,10 +183,14 @@ __global__ void __launch_bounds__(512) k_potf2_128(const Prob* __restrict__ prob
     if (fail_col >= 0) break;
     if (tid > j && tid < NB) A[j * S + tid] *= rdiag;
     __syncthreads();
-    const int w = NB - 1 - j;
-    for (int e = tid; e < w * w; e += blockDim.x) {
-      const int r = j + 1 + e % w, c = j + 1 + e / w;
-      if (r >= c) A[c * S + r] = fma(-A[j * S + r], A[j * S + c], A[c * S + r]);
+    // rank-1 update of the trailing lower triangle: thread (row r, group g)
+    // updates columns c = j+1+g, j+1+g+4, ... <= r
+    {
+      const int r = tid & (NB - 1), g = tid >> 7;
+      if (r > j) {
+        const double ljr = A[j * S + r];
+        for (int c = j + 1 + g; c <= r; c += 4) A[c * S + r] = fma(-ljr, A[j * S + c], A[c * S + r]);
+      }
     }
     __syncthreads();
   }
@@ -295,55 +296,86 @@ __global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, i
 }
 
 // ---------------------------------------------------------------------------
-// trailing update of the integer accumulators for one 128 x 64 output tile
+// trailing update of the integer accumulators: persistent, warp-specialised
 //
-// Accumulators are stored tile-major (128 x 64 tiles, column-major inside),
-// so one tile of each word is a contiguous 64 KB block: it is prefetched into
-// shared memory by the bulk-copy engine while the MMAs run, and the epilogue
-// adds to it without waiting on HBM.
+// Output tiles are 128 rows x 64 columns; a tile's 7 level sums occupy 448
+// TMEM columns.  Warp 8 (one lane) streams the digit planes of each k-chunk
+// of 16 by 5-D TMA into a 5-stage ring; warp 9 (one lane) issues the 28
+// tcgen05.mma of a chunk; warps 0-7 drain TMEM into registers, release it
+// (so the next tile's MMAs start), then add the tile into the int64/int32
+// accumulators in HBM while the tensor cores work on the next tile.
+//
+// Accumulator per element: W = hi * 2^24 + lo, hi int64, lo in [0, 2^24),
+// value = W * 2^(e_i + e_j - 62); tile-major storage (128 x 64 tiles,
+// column-major inside).  Tiles of a step are enumerated problem by problem
+// (prefix table from the host), column tile major, row tile minor.
 // ---------------------------------------------------------------------------
 constexpr int CH = 8;                                // k-chunks of 16 per 128-panel (one MMA each)
-constexpr uint32_t A_STAGE = NSLICE * 4096;          // 7 planes x 128 rows x 16 k x 2 B
-constexpr uint32_t B_STAGE = NSLICE * 2048;          // 7 planes x 64 rows x 16 k x 2 B
+constexpr int NSTAGE = 5;
+constexpr uint32_t A_STAGE = NSLICE * 4096;          // 7 planes x 2 k-groups x 128 rows x 16 B
+constexpr uint32_t B_STAGE = NSLICE * 2048;          // 7 planes x 2 k-groups x 64 rows x 16 B
 constexpr uint32_t STAGE = A_STAGE + B_STAGE;        // 43008 B
-constexpr uint32_t ACC_TILE = 128 * 64 * 8;          // one int64 word of a tile: 64 KB
-constexpr uint32_t UPD_SMEM = 2 * STAGE + 2 * ACC_TILE + 128;
+constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + 256;
+constexpr int UPD_THREADS = 320;
 
-__device__ __forceinline__ size_t acc_index(int i, int j, int nt) {
-  return ((size_t)((j >> 6) * nt + (i >> 7)) * 64 + (j & 63)) * 128 + (i & 127);
+__device__ __forceinline__ void tma_load_5d(void* dst, const void* tmap, int c0, int c1, int c2, int c3, int c4,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+      "%6}], [%7];" ::"r"(su32(dst)),
+      "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(su32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
 }
 
-__global__ void __launch_bounds__(256, 1) k_ozaki_update(const Prob* __restrict__ probs, int s) {
-  const Prob& P = probs[blockIdx.z];
-  if (P.mode != 1 || P.status[1]) return;
-  const int m = P.nt128 - s - 1;
-  if ((int)blockIdx.x >= m || (int)blockIdx.y >= 2 * m) return;
-  const int ti = s + 1 + blockIdx.x;            // 128-row tile
-  const int tj = 2 * (s + 1) + blockIdx.y;      // 64-column tile
-  if (tj / 2 > ti) return;                      // strictly upper
+// tile t of step s -> (problem, 128-row tile, 64-column tile); false if out of range
+__device__ __forceinline__ bool decode_tile(const Prob* __restrict__ probs, const int* __restrict__ prefix, int nprob,
+                                            int s, int t, int& p, int& ti, int& tj) {
+  if (t >= prefix[nprob]) return false;
+  int lo = 0, hi = nprob;  // largest p with prefix[p] <= t
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  p = lo;
+  const int m = probs[p].nt128 - s - 1;
+  int r = t - prefix[p];
+  // column-tile pair q (tj = 2(s+1)+2q, +1) holds 2 (m - q) tiles
+  int q = 0;
+  while (r >= 2 * (m - q)) {
+    r -= 2 * (m - q);
+    ++q;
+  }
+  const int half = r >= (m - q) ? 1 : 0;
+  const int rr = r - half * (m - q);
+  tj = 2 * (s + 1) + 2 * q + half;
+  ti = s + 1 + q + rr;
+  return true;
+}
+
+__global__ void __launch_bounds__(UPD_THREADS, 1)
+    k_ozaki_update(const Prob* __restrict__ probs, int nprob, int s, const int* __restrict__ prefix) {
   extern __shared__ __align__(1024) unsigned char smu[];
-  long long* acc_hi_s = reinterpret_cast<long long*>(smu + 2 * STAGE);
-  long long* acc_lo_s = reinterpret_cast<long long*>(smu + 2 * STAGE + ACC_TILE);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smu + 2 * STAGE + 2 * ACC_TILE);
-  uint64_t* empty = full + 2;
-  uint64_t* done = full + 4;
-  uint64_t* accbar = full + 5;
-  uint32_t* slot = reinterpret_cast<uint32_t*>(full + 6);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smu + NSTAGE * STAGE);
+  uint64_t* empty = full + NSTAGE;
+  uint64_t* tfull = full + 2 * NSTAGE;
+  uint64_t* tempty = tfull + 1;
+  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 2);
   __shared__ int s_abort;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const bool first = (s == 0);
-  const size_t tile_off = (size_t)(tj * P.nt128 + ti) * (128 * 64);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     s_abort = 0;
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < NSTAGE; ++k) {
       mbar_init(&full[k], 1);
       mbar_init(&empty[k], 1);
     }
-    mbar_init(done, 1);
-    mbar_init(accbar, 1);
+    mbar_init(tfull, 1);
+    mbar_init(tempty, 256);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 9) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -351,96 +383,160 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_update(const Prob* __restrict_
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tbase = *slot;
+  const int total = prefix[nprob];
 
-  const unsigned char* Ag = P.slices + (size_t)ti * NSLICE * SLICE_BYTES;
-  const unsigned char* Bg = P.slices + (size_t)(tj / 2) * NSLICE * SLICE_BYTES + (size_t)(tj % 2) * 1024;
-
-  if (tid == 0) {
-    if (!first) {
-      mbar_expect_tx(accbar, 2 * ACC_TILE);
-      bulk_g2s(acc_hi_s, P.acc_hi + tile_off, ACC_TILE, accbar);
-      bulk_g2s(acc_lo_s, P.acc_lo + tile_off, ACC_TILE, accbar);
-    }
-    auto load = [&](int c, int st) {
-      unsigned char* As = smu + st * STAGE;
-      unsigned char* Bs = As + A_STAGE;
-      mbar_expect_tx(&full[st], STAGE);
-      for (int p = 0; p < NSLICE; ++p) {
-        bulk_g2s(As + p * 4096, Ag + (size_t)p * SLICE_BYTES + (size_t)c * 4096, 4096, &full[st]);
-        for (int kq = 0; kq < 2; ++kq)
-          bulk_g2s(Bs + p * 2048 + kq * 1024, Bg + (size_t)p * SLICE_BYTES + (size_t)(2 * c + kq) * 2048, 1024,
-                   &full[st]);
-      }
-    };
-    load(0, 0);
-    load(1, 1);
-    bool ok = true;
-    for (int c = 0; c < CH && ok; ++c) {
-      const int st = c & 1;
-      ok = mbar_wait(&full[st], (c >> 1) & 1);
-      if (!ok) break;
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t As = su32(smu + st * STAGE);
-      const uint32_t Bs = As + A_STAGE;
-      for (int p = 0; p < NSLICE; ++p) {
-        const uint64_t ad = smem_desc(As + p * 4096, 2048, 128);
-        for (int q = 0; q + p < NSLICE; ++q) {
-          const uint64_t bd = smem_desc(Bs + q * 2048, 1024, 128);
-          mma_f16(tbase + (uint32_t)(p + q) * 64, ad, bd, (c == 0 && p == 0) ? 0u : 1u);
+  if (warp == 8) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      uint32_t g = 0;
+      for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        int p, ti, tj;
+        decode_tile(probs, prefix, nprob, s, t, p, ti, tj);
+        const Prob& P = probs[p];
+        if (P.status[1]) continue;
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_b) : "memory");
+        for (int c = 0; c < CH; ++c, ++g) {
+          const int st = g % NSTAGE;
+          if (!mbar_wait(&empty[st], ((g / NSTAGE) & 1) ^ 1)) {
+            s_abort = 1;
+            break;
+          }
+          unsigned char* As = smu + st * STAGE;
+          mbar_expect_tx(&full[st], STAGE);
+          tma_load_5d(As, P.tmap_a, 0, 0, 2 * c, 0, ti, &full[st]);
+          tma_load_5d(As + A_STAGE, P.tmap_b, 0, (tj & 1) * 2, 2 * c, 0, tj >> 1, &full[st]);
         }
-      }
-      mma_commit(&empty[st]);
-      if (c >= 1 && c + 1 < CH) {
-        const int pst = (c - 1) & 1;
-        ok = mbar_wait(&empty[pst], ((c - 1) >> 1) & 1);
-        if (ok) load(c + 1, pst);
+        if (s_abort) break;
       }
     }
-    mma_commit(done);
-    if (!ok) s_abort = 1;
-  }
-  bool fin = mbar_wait(done, 0);
-  if (!first) fin = fin && mbar_wait(accbar, 0);
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  if (!fin || s_abort) {
-    if (tid == 0) atomicExch(&P.status[2], 1);
+  } else if (warp == 9) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      uint32_t g = 0, it = 0;
+      const uint64_t adesc0 = smem_desc(su32(smu), 2048, 128);
+      const uint64_t bdesc0 = smem_desc(su32(smu) + A_STAGE, 1024, 128);
+      for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        int p, ti, tj;
+        decode_tile(probs, prefix, nprob, s, t, p, ti, tj);
+        if (probs[p].status[1]) continue;
+        if (!mbar_wait(tempty, (it & 1) ^ 1)) {
+          s_abort = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        bool ok = true;
+        for (int c = 0; c < CH; ++c, ++g) {
+          const int st = g % NSTAGE;
+          if (!mbar_wait(&full[st], (g / NSTAGE) & 1)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint64_t soff = (uint64_t)((st * STAGE) >> 4);
+#pragma unroll
+          for (int pp = 0; pp < NSLICE; ++pp) {
+#pragma unroll
+            for (int q = 0; q + pp < NSLICE; ++q) {
+              mma_f16(tbase + (uint32_t)(pp + q) * 64, adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
+                      bdesc0 + soff + (uint64_t)(q * 2048 >> 4), (c == 0 && pp == 0) ? 0u : 1u);
+            }
+          }
+          mma_commit(&empty[st]);
+        }
+        if (!ok) {
+          s_abort = 1;
+          break;
+        }
+        mma_commit(tfull);
+        ++it;
+      }
+    }
   } else {
-    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its rows) and the
-    // column half w / 4; 7 exact level sums -> two int64 words per element
-    const int r = (warp & 3) * 32 + (tid & 31);
-    const int h = warp >> 2;
-    long long* gh = P.acc_hi + tile_off;
-    long long* gl = P.acc_lo + tile_off;
-    for (int cc = 0; cc < 4; ++cc) {
-      const int col0 = h * 32 + cc * 8;
-      uint32_t v[NSLICE][8];
-      for (int l = 0; l < NSLICE; ++l) {
-        const uint32_t ta = tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(l * 64 + col0);
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                     : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]), "=r"(v[l][5]),
-                       "=r"(v[l][6]), "=r"(v[l][7])
-                     : "r"(ta));
+    // ---------------- epilogue (warps 0-7) ----------------
+    const int r = (warp & 3) * 32 + lane;  // TMEM lane = tile row
+    const int h = warp >> 2;               // column half
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    uint32_t it = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+      int p, ti, tj;
+      decode_tile(probs, prefix, nprob, s, t, p, ti, tj);
+      const Prob& P = probs[p];
+      if (P.status[1]) continue;
+      if (!mbar_wait(tfull, it & 1)) {
+        s_abort = 1;
+        break;
       }
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
-      for (int jj = 0; jj < 8; ++jj) {
-        long long S[NSLICE];
-        for (int l = 0; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
-        long long hi = S[0] * 65536 + S[1] * 256 + S[2];
-        long long lo = S[3] * 16777216 + S[4] * 65536 + S[5] * 256 + S[6];
-        const int idx = (col0 + jj) * 128 + r;
-        if (!first) {
-          hi += acc_hi_s[idx];
-          lo += acc_lo_s[idx];
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      long long hv[32];
+      int lv[32];
+#pragma unroll
+      for (int gq = 0; gq < 4; ++gq) {
+        const int col0 = h * 32 + gq * 8;
+        uint32_t v[NSLICE][8];
+#pragma unroll
+        for (int l = 0; l < NSLICE; ++l) {
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                       : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
+                         "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
+                       : "r"(tbase + lane_base + (uint32_t)(l * 64 + col0)));
         }
-        gh[idx] = hi;
-        gl[idx] = lo;
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+          long long S[NSLICE];
+#pragma unroll
+          for (int l = 0; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
+          // W = S0 2^48 + S1 2^40 + S2 2^32 + S3 2^24 + S4 2^16 + S5 2^8 + S6
+          const long long low = S[4] * 65536 + S[5] * 256 + S[6];  // |low| < 2^41
+          hv[gq * 8 + jj] = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
+          lv[gq * 8 + jj] = (int)(low & 0xFFFFFF);
+        }
+      }
+      // TMEM drained: let the next tile's MMAs start
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      mbar_arrive(tempty);
+      ++it;
+      const size_t tile = (size_t)(tj * P.nt128 + ti) * (128 * 64);
+      long long* gh = P.acc_hi + tile;
+      int* gl = P.acc_lo + tile;
+      const bool first = (s == 0);
+#pragma unroll
+      for (int gq = 0; gq < 4; ++gq) {
+        long long ah[8];
+        int al[8];
+        if (!first) {
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const int idx = (h * 32 + gq * 8 + jj) * 128 + r;
+            ah[jj] = gh[idx];
+            al[jj] = gl[idx];
+          }
+        }
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+          const int idx = (h * 32 + gq * 8 + jj) * 128 + r;
+          long long hi = hv[gq * 8 + jj];
+          long long lo = lv[gq * 8 + jj];
+          if (!first) {
+            hi += ah[jj];
+            lo += al[jj];
+            hi += lo >> 24;
+            lo &= 0xFFFFFF;
+          }
+          gh[idx] = hi;
+          gl[idx] = (int)lo;
+        }
       }
     }
   }
-  asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
+  if (s_abort && tid == 0) {
+    // a bounded wait gave up: flag every problem of this step
+    for (int q = 0; q < nprob; ++q) atomicExch(&probs[q].status[2], 1);
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == 9) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
 }
 
 // ---------------------------------------------------------------------------
@@ -467,6 +563,44 @@ __global__ void __launch_bounds__(256) k_border_update(const Prob* __restrict__ 
   }
   P.K[(size_t)j * ld + P.Nc] -= a0;
   if (P.nrhs > 1) P.K[(size_t)j * ld + P.Nc + 1] -= a1;
+}
+
+// ---------------------------------------------------------------------------
+// host: TMA tensor maps over a problem's digit-plane buffer
+// buffer layout: [row tile nt128][plane 7][k-group 16][row 128][8 fp16]; a (k-group, plane)
+// block is 2 KB contiguous
+// ---------------------------------------------------------------------------
+int encode_slice_maps(void* host_maps, const void* slices, int nt128) {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::mutex mu;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!fn) {
+      void* f = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+              cudaSuccess ||
+          q != cudaDriverEntryPointSuccess || !f)
+        return -1;
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }
+  }
+  // A (k-group, plane) block of 128 rows x 16 B is 2 KB contiguous: describe it
+  // as 4 rows of 256 fp16 (512 B) so each TMA request moves 512 B.
+  const cuuint64_t dims[5] = {256, 4, 16, (cuuint64_t)NSLICE, (cuuint64_t)nt128};
+  const cuuint64_t strides[4] = {512, 2048, (cuuint64_t)SLICE_BYTES, (cuuint64_t)NSLICE * SLICE_BYTES};
+  const cuuint32_t boxA[5] = {256, 4, 2, NSLICE, 1};   // 128 rows
+  const cuuint32_t boxB[5] = {256, 2, 2, NSLICE, 1};   // 64 rows
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  CUtensorMap* m = static_cast<CUtensorMap*>(host_maps);
+  CUresult r = fn(&m[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dims, strides, boxA, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return (int)r;
+  r = fn(&m[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dims, strides, boxB, es,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return (int)r;
 }
 
 // ---------------------------------------------------------------------------
@@ -525,12 +659,13 @@ cudaError_t launch_split(const Prob* probs, int nprob, int step, int max_nt128, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
+cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, const int* prefix,
+                                int total_tiles, int num_sms, cudaStream_t s) {
   cudaError_t e = set_attrs();
   if (e != cudaSuccess) return e;
-  const int m = max_nt128 - step - 1;
-  if (m <= 0) return cudaSuccess;
-  k_ozaki_update<<<dim3(m, 2 * m, nprob), 256, UPD_SMEM, s>>>(probs, step);
+  if (max_nt128 - step - 1 <= 0 || total_tiles <= 0) return cudaSuccess;
+  const int grid = total_tiles < num_sms ? total_tiles : num_sms;
+  k_ozaki_update<<<grid, UPD_THREADS, UPD_SMEM, s>>>(probs, nprob, step, prefix);
   return cudaGetLastError();
 }
 
