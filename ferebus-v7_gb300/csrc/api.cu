@@ -128,6 +128,8 @@ struct Workspace {
   int* acc_lo = nullptr;
   unsigned char* slices = nullptr;
   unsigned char* tmaps = nullptr;  // 2 x 128 B TMA tensor maps over slices
+  double* splanes = nullptr;       // theta-scaled planes (dot-product build)
+  double* norms = nullptr;
 };
 
 // Process-wide default trailing-update mode for contexts created from now on:
@@ -240,6 +242,8 @@ void fill_prob(Prob& p, const fgpu_ctx* c, const double* theta_d, const Workspac
   p.slices = ws.slices;
   p.tmap_a = ws.tmaps;
   p.tmap_b = ws.tmaps ? ws.tmaps + 128 : nullptr;
+  p.splanes = ws.splanes;
+  p.norms = ws.norms;
 }
 
 int build_sched(const std::vector<int>& nt128, UpdSched& u, std::vector<void*>* track) {
@@ -295,15 +299,24 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
                  const UpdSched* us = nullptr) {
   long long n = 0;
   CK(cudaMemsetAsync(status_base, 0, status_bytes, s));
-  STAGE(0, launch_build(probs_d, nprob, max_nsteps, max_nplanes, s));
   if (mode == 1) {
     // 128-wide panels; max_nsteps counts 64-column tiles
     const int nt = max_nsteps / 2, max_nc = max_nsteps * TB;
+    STAGE(0, launch_prep_planes(probs_d, nprob, max_nc, s));
+    STAGE(0, launch_build_dot(probs_d, nprob, max_nsteps, max_nplanes, s));
     STAGE(0, launch_scales(probs_d, nprob, max_nc, s));
     for (int step = 0; step < nt; ++step) {
       if (step > 0) STAGE(5, launch_panel_prep(probs_d, nprob, step, max_nc, s));
-      STAGE(1, launch_potf2_128(probs_d, nprob, step, s));
-      STAGE(2, launch_trsm128(probs_d, nprob, step, nt, s));
+      // first 64-column half: FP64 diagonal factor + panel solve
+      STAGE(1, launch_potf2(probs_d, nprob, 2 * step, s));
+      STAGE(2, launch_trsm(probs_d, nprob, 2 * step, max_nsteps, s));
+      // coupling into the second half on the tensor cores
+      STAGE(6, launch_split_half(probs_d, nprob, step, nt, s));
+      STAGE(6, launch_gemm_half(probs_d, nprob, step, nt, s));
+      STAGE(7, launch_border_half(probs_d, nprob, step, s));
+      // second half
+      STAGE(1, launch_potf2(probs_d, nprob, 2 * step + 1, s));
+      STAGE(2, launch_trsm(probs_d, nprob, 2 * step + 1, max_nsteps, s));
       if (step + 1 < nt) {
         STAGE(6, launch_split(probs_d, nprob, step, nt, s));
         STAGE(3, launch_ozaki_update(probs_d, nprob, step, nt, us->prefix_dev + (size_t)step * us->stride,
@@ -315,6 +328,7 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
     if (kernels) *kernels = n;
     return 0;
   }
+  STAGE(0, launch_build(probs_d, nprob, max_nsteps, max_nplanes, s));
   for (int step = 0; step < max_nsteps; ++step) {
     STAGE(1, launch_potf2(probs_d, nprob, step, s));
     STAGE(2, launch_trsm(probs_d, nprob, step, max_nsteps, s));
@@ -357,6 +371,9 @@ int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track)
     CK(cudaMalloc(&ws.acc_hi, sizeof(long long) * nc * nc));
     CK(cudaMalloc(&ws.acc_lo, sizeof(int) * nc * nc));
     CK(cudaMalloc(&ws.slices, (size_t)c->nt128 * NSLICE * SLICE_BYTES));
+    CK(cudaMalloc(&ws.splanes, sizeof(double) * (size_t)std::max(c->spec.nplanes, 1) * nc));
+    CK(cudaMalloc(&ws.norms, sizeof(double) * (size_t)MAX_LEAF * nc));
+    CK(cudaMemset(ws.norms, 0, sizeof(double) * (size_t)MAX_LEAF * nc));
     CK(cudaMalloc(&ws.tmaps, 256));
     alignas(64) unsigned char maps[256];
     const int er = encode_slice_maps(maps, ws.slices, c->nt128);
@@ -365,7 +382,8 @@ int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track)
   }
   if (track) {
     for (void* q : {(void*)ws.K, (void*)ws.logdet_part, (void*)ws.out, (void*)ws.z, (void*)ws.escale,
-                    (void*)ws.pw2, (void*)ws.acc_hi, (void*)ws.acc_lo, (void*)ws.slices, (void*)ws.tmaps})
+                    (void*)ws.pw2, (void*)ws.acc_hi, (void*)ws.acc_lo, (void*)ws.slices, (void*)ws.tmaps,
+                    (void*)ws.splanes, (void*)ws.norms})
       if (q) track->push_back(q);
   }
   return 0;
@@ -385,6 +403,8 @@ void free_worker(Worker* w) {
   cudaFree(w->ws.acc_lo);
   cudaFree(w->ws.slices);
   cudaFree(w->ws.tmaps);
+  cudaFree(w->ws.splanes);
+  cudaFree(w->ws.norms);
   cudaFree(w->theta_d);
   cudaFree(w->prob_d);
   cudaFree(w->sched.prefix_dev);
@@ -488,15 +508,35 @@ int fgpu_create(fgpu_ctx** out, int N, int d, const double* X, const double* y, 
   c->optimise_noise = optimise_noise ? 1 : 0;
   c->nkparams = c->spec.nkparams;
   c->ntheta = c->nkparams + c->optimise_noise;
-  // feature planes, plane-major, padded to Nc
+  // feature planes, plane-major, padded to Nc.  FP64 mode: x, or the
+  // half-angle pair sin(x/2), cos(x/2) for periodic dims.  Tensor-core mode
+  // (dot-product build): rbf dims centred on their mean, periodic dims as
+  // the pair cos(x), sin(x), rbf-cyclic dims raw.
   const int np = c->spec.nplanes;
   std::vector<double> planes((size_t)std::max(np, 1) * c->Nc, 0.0);
+  std::vector<int> plane_leaf(np, 0);
+  for (int l = 0; l < c->spec.nleaf; ++l) {
+    const Leaf& L = c->spec.leaf[l];
+    const int cnt = L.type == FGPU_PERIODIC ? 2 * L.n : (L.type == FGPU_LINEAR || L.type == FGPU_CONSTANT ? 0 : L.n);
+    for (int q = 0; q < cnt; ++q) plane_leaf[L.plane0 + q] = L.type;
+  }
   for (int p = 0; p < np; ++p) {
     const double* col = X + (size_t)plane_dim[p] * N;  // X(:, dim), column-major
     double* dst = planes.data() + (size_t)p * c->Nc;
+    if (c->mode == 1 && plane_leaf[p] == FGPU_RBF) {
+      double mean = 0.0;
+      for (int i = 0; i < N; ++i) mean += col[i];
+      mean /= N;
+      for (int i = 0; i < N; ++i) dst[i] = col[i] - mean;
+      continue;
+    }
     for (int i = 0; i < N; ++i) {
       const double x = col[i];
-      if (plane_kind[p] == 1)
+      if (c->mode == 1 && plane_kind[p] == 1)
+        dst[i] = std::cos(x);
+      else if (c->mode == 1 && plane_kind[p] == 2)
+        dst[i] = std::sin(x);
+      else if (plane_kind[p] == 1)
         dst[i] = std::sin(x / 2.0);
       else if (plane_kind[p] == 2)
         dst[i] = std::cos(x / 2.0);

@@ -244,6 +244,175 @@ __global__ void __launch_bounds__(256) k_build(const Prob* __restrict__ probs) {
 }
 
 // ---------------------------------------------------------------------------
+// dot-product form of the kernel-matrix build (tensor-core mode)
+//
+// With u_ik = sqrt(l_k) (x_ik - xbar_k) and a_i = sum_k u_ik^2,
+//   sum_k l_k (x_ik - x_jk)^2 = a_i + a_j - 2 <u_i, u_j>,
+// and with v_ik = sqrt(l_k) (cos x_ik, sin x_ik),
+//   2 sum_k l_k sin^2((x_ik - x_jk) / 2) = sum_k l_k - <v_i, v_j>,
+// so an rbf or periodic leaf costs one FP64 FMA per feature and pair instead
+// of three or four.  The rounding error of the exponent is about u * a_i
+// (absolute) on centred features, the size of its own rounding in the direct
+// form for the well separated pairs that dominate, and it vanishes on the
+// diagonal, which is set exactly (x_i = x_j gives a factor 1).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_prep_planes(const Prob* __restrict__ probs) {
+  const Prob& P = probs[blockIdx.z];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int l = blockIdx.y;
+  if (P.mode != 1 || i >= P.Nc) return;
+  const Spec& sp = *P.spec;
+  if (l >= sp.nleaf) return;
+  const Leaf& L = sp.leaf[l];
+  const size_t nc = (size_t)P.Nc;
+  if (L.type == L_RBF) {
+    double a = 0.0;
+    for (int k = 0; k < L.n; ++k) {
+      const double w = exp(0.5 * P.theta[L.param0 + k]);  // sqrt(exp(theta))
+      const double u = w * P.planes[(size_t)(L.plane0 + k) * nc + i];
+      P.splanes[(size_t)(L.plane0 + k) * nc + i] = u;
+      a = fma(u, u, a);
+    }
+    P.norms[(size_t)l * nc + i] = a;
+  } else if (L.type == L_PERIODIC) {
+    for (int k = 0; k < L.n; ++k) {
+      const double w = 1.0 / exp(P.theta[L.param0 + k]);  // sqrt((1 / exp(theta))^2)
+      for (int t = 0; t < 2; ++t) {
+        const size_t o = (size_t)(L.plane0 + 2 * k + t) * nc + i;
+        P.splanes[o] = w * P.planes[o];
+      }
+    }
+  } else if (L.type == L_RBF_CYCLIC) {
+    for (int k = 0; k < L.n; ++k) {
+      const size_t o = (size_t)(L.plane0 + k) * nc + i;
+      P.splanes[o] = P.planes[o];
+    }
+  }
+}
+
+size_t build_dot_smem_bytes(int nplanes) {
+  return (size_t)2 * (nplanes + MAX_LEAF) * TB * sizeof(double) + 64;
+}
+
+__global__ void __launch_bounds__(256) k_build_dot(const Prob* __restrict__ probs) {
+  const Prob& P = probs[blockIdx.z];
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (P.mode != 1 || tj >= P.nsteps || ti > P.nsteps || ti < tj) return;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const Spec& sp = *P.spec;
+  const int np = sp.nplanes;
+  const int nl = sp.nleaf;
+  double* Pi = reinterpret_cast<double*>(smem_raw);      // np x 64 planes, row points
+  double* Pj = Pi + (size_t)np * TB;                      // column points
+  double* Ni = Pj + (size_t)np * TB;                      // nl x 64 norms, row points
+  double* Nj = Ni + (size_t)MAX_LEAF * TB;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(Nj + (size_t)MAX_LEAF * TB);
+  __shared__ double ls[MAX_PARAMS];
+  __shared__ double leaf_c[MAX_LEAF];  // sum of l (periodic) or sum of 1/c (linear)
+  __shared__ int s_fail;
+  const int tid = threadIdx.x;
+  const bool border = (ti == P.nsteps);
+  const int i0 = ti * TB, j0 = tj * TB;
+  const size_t nc = (size_t)P.Nc;
+  if (tid == 0) {
+    s_fail = 0;
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const uint32_t per = TB * sizeof(double);
+    const uint32_t nrows = (uint32_t)(np + nl);
+    mbar_arrive_expect_tx(bar, per * nrows * (border ? 1 : 2));
+    for (int p = 0; p < np; ++p) {
+      bulk_g2s(Pj + p * TB, P.splanes + (size_t)p * nc + j0, per, bar);
+      if (!border) bulk_g2s(Pi + p * TB, P.splanes + (size_t)p * nc + i0, per, bar);
+    }
+    for (int l = 0; l < nl; ++l) {
+      bulk_g2s(Nj + l * TB, P.norms + (size_t)l * nc + j0, per, bar);
+      if (!border) bulk_g2s(Ni + l * TB, P.norms + (size_t)l * nc + i0, per, bar);
+    }
+  }
+  for (int k = tid; k < sp.nkparams; k += blockDim.x) {
+    int type = L_CONSTANT;
+    for (int l = 0; l < nl; ++l) {
+      const int cnt = sp.leaf[l].type == L_CONSTANT ? 1 : sp.leaf[l].n;
+      if (k >= sp.leaf[l].param0 && k < sp.leaf[l].param0 + cnt) type = sp.leaf[l].type;
+    }
+    ls[k] = transform_param(type, P.theta[k]);
+  }
+  __syncthreads();
+  if (tid < nl) {
+    double acc = 0.0;
+    const Leaf& L = sp.leaf[tid];
+    if (L.type == L_LINEAR)
+      for (int k = 0; k < L.n; ++k) acc += 1.0 / ls[L.param0 + k];
+    else if (L.type == L_PERIODIC)
+      for (int k = 0; k < L.n; ++k) acc += ls[L.param0 + k];
+    leaf_c[tid] = acc;
+  }
+  if (!mbar_wait_bounded(bar, 0)) s_fail = 1;
+  __syncthreads();
+  if (s_fail) {
+    if (tid == 0) atomicExch(&P.status[2], 1);
+    return;
+  }
+  const double noise = P.optimise_noise ? P.theta[sp.nkparams] : P.noise;
+  const int r0 = (tid & 31) * 2;
+  const int c0 = (tid >> 5) * 8;
+  double* K = P.K;
+  const size_t ld = (size_t)P.ld;
+  for (int cc = 0; cc < 8; ++cc) {
+    const int c = c0 + cc, j = j0 + c;
+    double v[2];
+    for (int a = 0; a < 2; ++a) {
+      const int r = r0 + a, i = i0 + r;
+      double val = 0.0;
+      if (border) {
+        if (j < P.N && r < P.nrhs)
+          val = (r == 0) ? ((P.likelihood == 1) ? P.y[j] : P.y[j] - P.mu[j]) : 1.0;
+      } else if (i < P.N && j < P.N) {
+        if (i >= j) {
+          double stk[MAX_LEAF];
+          int top = 0;
+          for (int t = 0; t < sp.npost; ++t) {
+            const int tok = sp.post[t];
+            if (tok >= 0) {
+              const Leaf& L = sp.leaf[tok];
+              double lv;
+              if (L.type == L_RBF) {
+                double dot = 0.0;
+                for (int k = 0; k < L.n; ++k) dot = fma(Pi[(L.plane0 + k) * TB + r], Pj[(L.plane0 + k) * TB + c], dot);
+                const double e = (i == j) ? 0.0 : (Ni[tok * TB + r] + Nj[tok * TB + c]) - 2.0 * dot;
+                lv = exp(-0.5 * e);
+              } else if (L.type == L_PERIODIC) {
+                double dot = 0.0;
+                for (int k = 0; k < 2 * L.n; ++k)
+                  dot = fma(Pi[(L.plane0 + k) * TB + r], Pj[(L.plane0 + k) * TB + c], dot);
+                lv = (i == j) ? 1.0 : exp(dot - leaf_c[tok]);
+              } else {
+                lv = leaf_value(L, Pi, Pj, r, c, ls, sp.cyclic, leaf_c[tok]);
+              }
+              stk[top++] = lv;
+            } else {
+              const double b = stk[--top];
+              const double a2 = stk[--top];
+              stk[top++] = (tok == P_SUM) ? a2 + b : a2 * b;
+            }
+          }
+          val = stk[0];
+          if (i == j) val = val + noise * 1.0;
+        }
+      } else {
+        val = (i == j) ? 1.0 : 0.0;
+      }
+      v[a] = val;
+    }
+    *reinterpret_cast<double2*>(K + (size_t)j * ld + i0 + r0) = make_double2(v[0], v[1]);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // diagonal block factorisation (unblocked, right-looking) + log-det partial
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_potf2(const Prob* __restrict__ probs, int step) {
@@ -552,6 +721,25 @@ cudaError_t launch_build(const Prob* probs, int nprob, int max_nsteps, int max_n
   }
   dim3 grid(max_nsteps + 1, max_nsteps, nprob);
   k_build<<<grid, 256, smem, s>>>(probs);
+  return cudaGetLastError();
+}
+
+static int g_build_dot_attr_set = 0;
+
+cudaError_t launch_prep_planes(const Prob* probs, int nprob, int max_nc, cudaStream_t s) {
+  k_prep_planes<<<dim3((max_nc + 255) / 256, MAX_LEAF, nprob), 256, 0, s>>>(probs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_dot(const Prob* probs, int nprob, int max_nsteps, int max_nplanes, cudaStream_t s) {
+  if (!g_build_dot_attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_build_dot, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)build_dot_smem_bytes(MAX_PLANES));
+    if (e != cudaSuccess) return e;
+    g_build_dot_attr_set = 1;
+  }
+  dim3 grid(max_nsteps + 1, max_nsteps, nprob);
+  k_build_dot<<<grid, 256, build_dot_smem_bytes(max_nplanes), s>>>(probs);
   return cudaGetLastError();
 }
 

@@ -73,6 +73,9 @@ struct Prob {
   unsigned char* slices;          // nt128 x 7 x 32 KB: fp16 digit planes of the current panel
   const void* tmap_a;             // TMA tensor map over slices, box 8 x 128 rows x 2 kgroups x 7 planes
   const void* tmap_b;             // same, box of 64 rows
+  // dot-product kernel build (mode 1): planes scaled by sqrt(l_k) per evaluation
+  double* splanes;                // nplanes x Nc
+  double* norms;                  // MAX_LEAF x Nc: sum_k u_ik^2 of rbf leaves
 };
 
 // Encode the two 5-D TMA tensor maps of a problem's digit-plane buffer into
@@ -83,6 +86,10 @@ int encode_slice_maps(void* host_maps, const void* slices, int nt128);
 // and index it by blockIdx.y; problems whose geometry does not reach the
 // current step exit immediately, so ragged batches share one launch.
 cudaError_t launch_build(const Prob* probs, int nprob, int max_nsteps, int max_nplanes, cudaStream_t s);
+// mode 1: per-evaluation scaled planes, then the dot-product form of the build
+cudaError_t launch_prep_planes(const Prob* probs, int nprob, int max_nc, cudaStream_t s);
+cudaError_t launch_build_dot(const Prob* probs, int nprob, int max_nsteps, int max_nplanes, cudaStream_t s);
+size_t build_dot_smem_bytes(int nplanes);
 cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s);
 cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s);
 cudaError_t launch_update(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s);
@@ -105,6 +112,12 @@ cudaError_t launch_split(const Prob* probs, int nprob, int step, int max_nt128, 
 cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, const int* prefix,
                                 int total_tiles, int num_sms, cudaStream_t s);
 cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
+// two 64-column halves per 128-panel: digit planes of the first half (rows
+// from the panel's own row tile), their tensor-core coupling into the second
+// half, and the FP64 coupling of the right-hand-side rows
+cudaError_t launch_split_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
+cudaError_t launch_gemm_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
+cudaError_t launch_border_half(const Prob* probs, int nprob, int step, cudaStream_t s);
 
 // api.cu hooks for other translation units.
 int internal_compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>& plane_dim,

@@ -266,9 +266,9 @@ __global__ void __launch_bounds__(256) k_trsm128(const Prob* __restrict__ probs,
 // digit planes of the panel rows below the diagonal block
 // layout per 128-row tile and digit p: [kgroup 16][row 128][8 k] fp16
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, int s) {
+__global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, int s, int ti0) {
   const Prob& P = probs[blockIdx.z];
-  const int ti = s + 1 + blockIdx.x;
+  const int ti = ti0 + blockIdx.x;
   if (P.mode != 1 || ti >= P.nt128 || P.status[1]) return;
   const int r = threadIdx.x, kg = blockIdx.y;
   const int i = ti * NB + r;
@@ -278,7 +278,10 @@ __global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, i
   int d[NSLICE][8];
   bool bad = false;
   for (int kk = 0; kk < 8; ++kk) {
-    long long F = to_fixed55(col[(size_t)kk * ld], e, &bad);
+    // only the lower triangle belongs to the factor (rows of the panel's own
+    // diagonal block carry stale values above the diagonal)
+    const double x = (s * NB + kg * 8 + kk > i) ? 0.0 : col[(size_t)kk * ld];
+    long long F = to_fixed55(x, e, &bad);
     for (int p = NSLICE - 1; p >= 1; --p) {
       const int b = (int)(signed char)(F & 0xFF);
       d[p][kk] = b;
@@ -540,6 +543,120 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
+// coupling of the two 64-column halves of panel s on the tensor cores:
+// K[i, c0+64+j] -= sum_{k<64} L[i, c0+k] L[c0+64+j, c0+k] for rows i >= c0+64,
+// from the digit planes of the first half (k-groups 0..7).  One CTA per
+// 128-row tile; the exact level sums are converted to FP64 once.
+// ---------------------------------------------------------------------------
+constexpr uint32_t HALF_SMEM = 4 * STAGE + 128;
+
+__global__ void __launch_bounds__(128, 1) k_gemm_half(const Prob* __restrict__ probs, int s) {
+  const Prob& P = probs[blockIdx.y];
+  const int ti = s + blockIdx.x;
+  if (P.mode != 1 || ti >= P.nt128 || P.status[1]) return;
+  extern __shared__ __align__(1024) unsigned char smh[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smh + 4 * STAGE);
+  uint64_t* done = full + 1;
+  uint32_t* slot = reinterpret_cast<uint32_t*>(full + 2);
+  __shared__ int s_ok;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid == 0) {
+    s_ok = 1;
+    mbar_init(full, 1);
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_b) : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tbase = *slot;
+  if (tid == 0) {
+    mbar_expect_tx(full, 4 * STAGE);
+    for (int c = 0; c < 4; ++c) {
+      unsigned char* As = smh + c * STAGE;
+      tma_load_5d(As, P.tmap_a, 0, 0, 2 * c, 0, ti, full);
+      tma_load_5d(As + A_STAGE, P.tmap_b, 0, 2, 2 * c, 0, s, full);  // rows c0+64 .. c0+127
+    }
+    bool ok = mbar_wait(full, 0);
+    if (ok) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint64_t adesc0 = smem_desc(su32(smh), 2048, 128);
+      const uint64_t bdesc0 = smem_desc(su32(smh) + A_STAGE, 1024, 128);
+      for (int c = 0; c < 4; ++c) {
+        const uint64_t soff = (uint64_t)((c * STAGE) >> 4);
+#pragma unroll
+        for (int pp = 0; pp < NSLICE; ++pp)
+#pragma unroll
+          for (int q = 0; q + pp < NSLICE; ++q)
+            mma_f16(tbase + (uint32_t)(pp + q) * 64, adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
+                    bdesc0 + soff + (uint64_t)(q * 2048 >> 4), (c == 0 && pp == 0) ? 0u : 1u);
+      }
+    }
+    mma_commit(done);
+    if (!ok) s_ok = 0;
+  }
+  const bool fin = mbar_wait(done, 0);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (!fin || !s_ok) {
+    if (tid == 0) atomicExch(&P.status[2], 1);
+  } else {
+    const int c0 = s * NB;
+    const int i = ti * NB + tid;  // TMEM lane = tile row
+    const bool live = i >= c0 + 64 && i < P.Nc;
+    const double pi = P.pw2[i < P.Nc ? i : 0];
+    const size_t ld = (size_t)P.ld;
+    for (int g = 0; g < 8; ++g) {
+      uint32_t v[NSLICE][8];
+#pragma unroll
+      for (int l = 0; l < NSLICE; ++l)
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]), "=r"(v[l][5]),
+                       "=r"(v[l][6]), "=r"(v[l][7])
+                     : "r"(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * 64 + g * 8)));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      if (live) {
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+          long long S[NSLICE];
+#pragma unroll
+          for (int l = 0; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
+          const long long low = S[4] * 65536 + S[5] * 256 + S[6];
+          const long long hi = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
+          const double w = fma((double)hi, 16777216.0, (double)(low & 0xFFFFFF));
+          const int j = c0 + 64 + g * 8 + jj;
+          double* kp = P.K + (size_t)j * ld + i;
+          *kp = *kp - w * pi * P.pw2[j];
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
+}
+
+// the same coupling for the right-hand-side rows (FP64)
+__global__ void __launch_bounds__(128) k_border_half(const Prob* __restrict__ probs, int s) {
+  const Prob& P = probs[blockIdx.x];
+  if (P.mode != 1 || s >= P.nt128 || P.status[1]) return;
+  const int q = threadIdx.x >> 6, jj = threadIdx.x & 63;
+  if (q >= P.nrhs) return;
+  const size_t ld = (size_t)P.ld;
+  const int c0 = s * NB;
+  const int j = c0 + 64 + jj;
+  double a = 0.0;
+  for (int k = 0; k < 64; ++k) a = fma(P.K[(size_t)(c0 + k) * ld + P.Nc + q], P.K[(size_t)(c0 + k) * ld + j], a);
+  P.K[(size_t)j * ld + P.Nc + q] -= a;
+}
+
+// ---------------------------------------------------------------------------
 // right-hand-side rows: C_qj -= sum_k Z_qk L_jk over the panel (FP64)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_border_update(const Prob* __restrict__ probs, int s) {
@@ -620,6 +737,9 @@ static cudaError_t set_attrs() {
   if ((e = cudaFuncSetAttribute(k_ozaki_update, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM)) !=
       cudaSuccess)
     return e;
+  if ((e = cudaFuncSetAttribute(k_gemm_half, cudaFuncAttributeMaxDynamicSharedMemorySize, HALF_SMEM)) !=
+      cudaSuccess)
+    return e;
   g_attr = true;
   return cudaSuccess;
 }
@@ -655,7 +775,28 @@ cudaError_t launch_trsm128(const Prob* probs, int nprob, int step, int max_nt128
 cudaError_t launch_split(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
   const int m = max_nt128 - step - 1;
   if (m <= 0) return cudaSuccess;
-  k_split<<<dim3(m, NB / 8, nprob), 128, 0, s>>>(probs, step);
+  k_split<<<dim3(m, NB / 8, nprob), 128, 0, s>>>(probs, step, step + 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
+  const int m = max_nt128 - step;
+  if (m <= 0) return cudaSuccess;
+  k_split<<<dim3(m, NB / 16, nprob), 128, 0, s>>>(probs, step, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
+  cudaError_t e = set_attrs();
+  if (e != cudaSuccess) return e;
+  const int m = max_nt128 - step;
+  if (m <= 0) return cudaSuccess;
+  k_gemm_half<<<dim3(m, nprob), 128, HALF_SMEM, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_border_half(const Prob* probs, int nprob, int step, cudaStream_t s) {
+  k_border_half<<<nprob, 128, 0, s>>>(probs, step);
   return cudaGetLastError();
 }
 
