@@ -171,9 +171,26 @@ struct Worker {
   UpdSched sched;
 };
 
+// Adjoint workspace (FP64 geometry): K with the right-hand-side tile and N
+// identity rows below it, K^-1, per-CTA partials.
+struct GradWS {
+  int Nc = 0, ld = 0, nsteps = 0, nrt = 0;
+  Workspace ws;
+  double* kinv = nullptr;
+  double* gpart = nullptr;
+  double* theta_d = nullptr;
+  double* g_d = nullptr;
+  Prob* prob_d = nullptr;
+  cudaStream_t stream = nullptr;
+  double* h_stage = nullptr;  // pinned: out(8) | g(ntheta) | status (as ints)
+};
+
 struct fgpu_ctx {
   int device = 0;
   int mode = 1;
+  double* planes64_d = nullptr;  // FP64-mode planes (x; sin(x/2), cos(x/2)) for the adjoint
+  GradWS* grad = nullptr;
+  std::mutex grad_mu;
   int nt128 = 0;
   int N = 0, d = 0, Nc = 0, ld = 0, nsteps = 0, nrhs = 1, likelihood = 0, optimise_noise = 0;
   int nkparams = 0, ntheta = 0;
@@ -551,6 +568,21 @@ int fgpu_create(fgpu_ctx** out, int N, int d, const double* X, const double* y, 
   }
   CK(cudaMalloc(&c->planes_d, planes.size() * sizeof(double)));
   CK(cudaMemcpy(c->planes_d, planes.data(), planes.size() * sizeof(double), cudaMemcpyHostToDevice));
+  // FP64-mode planes for the adjoint (64-padded), whatever the context's mode
+  {
+    const int nc64 = round_up(N, TB);
+    std::vector<double> p64((size_t)std::max(np, 1) * nc64, 0.0);
+    for (int p = 0; p < np; ++p) {
+      const double* col = X + (size_t)plane_dim[p] * N;
+      double* dst = p64.data() + (size_t)p * nc64;
+      for (int i = 0; i < N; ++i) {
+        const double x = col[i];
+        dst[i] = plane_kind[p] == 1 ? std::sin(x / 2.0) : (plane_kind[p] == 2 ? std::cos(x / 2.0) : x);
+      }
+    }
+    CK(cudaMalloc(&c->planes64_d, p64.size() * sizeof(double)));
+    CK(cudaMemcpy(c->planes64_d, p64.data(), p64.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
   CK(cudaMalloc(&c->y_d, c->Nc * sizeof(double)));
   CK(cudaMemcpy(c->y_d, yv.data(), c->Nc * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&c->mu_d, c->Nc * sizeof(double)));
@@ -589,6 +621,17 @@ void fgpu_destroy(fgpu_ctx* ctx) {
   cudaGetDevice(&prev);
   cudaSetDevice(ctx->device);
   for (Worker* w : ctx->workers) free_worker(w);
+  if (ctx->grad) {
+    GradWS* g = ctx->grad;
+    for (void* q : {(void*)g->ws.K, (void*)g->ws.logdet_part, (void*)g->ws.status, (void*)g->ws.out,
+                    (void*)g->ws.z, (void*)g->kinv, (void*)g->gpart, (void*)g->theta_d, (void*)g->g_d,
+                    (void*)g->prob_d})
+      cudaFree(q);
+    if (g->h_stage) cudaFreeHost(g->h_stage);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+  }
+  cudaFree(ctx->planes64_d);
   cudaFree(ctx->planes_d);
   cudaFree(ctx->y_d);
   cudaFree(ctx->mu_d);
@@ -633,14 +676,107 @@ int fgpu_loglik(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, int*
   return 0;
 }
 
+namespace {
+int make_grad_ws(fgpu_ctx* c, GradWS** out) {
+  std::unique_ptr<GradWS> g(new (std::nothrow) GradWS());
+  if (!g) return fail(FGPU_ENOMEM, "adjoint workspace");
+  g->Nc = round_up(c->N, TB);
+  g->nsteps = g->Nc / TB;
+  g->ld = 2 * g->Nc + TB;
+  g->nrt = g->ld / TB;
+  const size_t nc = (size_t)g->Nc;
+  CK(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+  CK(cudaMalloc(&g->ws.K, sizeof(double) * (size_t)g->ld * nc));
+  CK(cudaMalloc(&g->ws.logdet_part, sizeof(double) * (g->nsteps + 1)));
+  CK(cudaMalloc(&g->ws.status, sizeof(int) * 4));
+  CK(cudaMalloc(&g->ws.out, sizeof(double) * 8));
+  CK(cudaMalloc(&g->ws.z, sizeof(double) * nc));
+  CK(cudaMalloc(&g->kinv, sizeof(double) * nc * nc));
+  CK(cudaMalloc(&g->gpart, sizeof(double) * (size_t)g->nsteps * g->nsteps * GRAD_SLOTS));
+  CK(cudaMalloc(&g->theta_d, sizeof(double) * (c->ntheta + 1)));
+  CK(cudaMalloc(&g->g_d, sizeof(double) * (c->ntheta + 1)));
+  CK(cudaMalloc(&g->prob_d, sizeof(Prob)));
+  CK(cudaMallocHost(&g->h_stage, sizeof(double) * (c->ntheta + 16)));
+  Prob p;
+  memset(&p, 0, sizeof(p));
+  p.N = c->N;
+  p.Nc = g->Nc;
+  p.ld = g->ld;
+  p.nsteps = g->nsteps;
+  p.nrt = g->nrt;
+  p.nrhs = c->nrhs;
+  p.likelihood = c->likelihood;
+  p.optimise_noise = c->optimise_noise;
+  p.nkparams = c->nkparams;
+  p.noise = c->noise;
+  p.planes = c->planes64_d;
+  p.y = c->y_d;
+  p.mu = c->mu_d;
+  p.spec = c->spec_d;
+  p.theta = g->theta_d;
+  p.K = g->ws.K;
+  p.logdet_part = g->ws.logdet_part;
+  p.status = g->ws.status;
+  p.out = g->ws.out;
+  p.z = g->ws.z;
+  p.mode = 0;
+  p.kinv = g->kinv;
+  p.gpart = g->gpart;
+  CK(cudaMemcpy(g->prob_d, &p, sizeof(Prob), cudaMemcpyHostToDevice));
+  *out = g.release();
+  return 0;
+}
+}  // namespace
+
 int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, double* dll, int* info) {
-  (void)ctx;
-  (void)theta;
-  (void)ntheta;
-  (void)ll;
-  (void)dll;
-  (void)info;
-  return fail(FGPU_EINVAL, "fgpu_grad: adjoint not available in this build");
+  t_err.clear();
+  t_launches = 0;
+  if (!ctx || !theta || !ll || !dll || !info) return fail(FGPU_EINVAL, "NULL argument");
+  if (ntheta != ctx->ntheta) return fail(FGPU_EINVAL, "ntheta=%d, context expects %d", ntheta, ctx->ntheta);
+  for (int k = 0; k < ntheta; ++k)
+    if (!std::isfinite(theta[k])) return fail(FGPU_EINVAL, "theta[%d] is not finite", k);
+  CK(cudaSetDevice(ctx->device));
+  std::lock_guard<std::mutex> lk(ctx->grad_mu);
+  if (!ctx->grad) {
+    GradWS* g = nullptr;
+    int rc = make_grad_ws(ctx, &g);
+    if (rc) return rc;
+    ctx->grad = g;
+  }
+  GradWS* g = ctx->grad;
+  cudaStream_t s = g->stream;
+  memcpy(g->h_stage, theta, sizeof(double) * ntheta);
+  CK(cudaMemcpyAsync(g->theta_d, g->h_stage, sizeof(double) * ntheta, cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(g->ws.status, 0, sizeof(int) * 4, s));
+  long long n = 0;
+  CK(launch_build(g->prob_d, 1, g->nsteps, ctx->spec.nplanes, s));
+  CK(launch_identity_border(g->prob_d, g->Nc, s));
+  n += 2;
+  for (int step = 0; step < g->nsteps; ++step) {
+    CK(launch_potf2(g->prob_d, 1, step, s));
+    CK(launch_trsm(g->prob_d, 1, step, g->nsteps, s, g->nrt));
+    CK(launch_update(g->prob_d, 1, step, g->nsteps, s, g->nrt));
+    n += 3;
+  }
+  CK(launch_finalize(g->prob_d, 1, s));
+  ++n;
+  CK(launch_backsolve(g->prob_d, 1, g->nsteps, nullptr, s, &n));
+  CK(launch_syrk_inv(g->prob_d, g->nsteps, s));
+  ++n;
+  CK(enqueue_grad_passes(g->prob_d, g->nsteps, ctx->nkparams, ctx->optimise_noise, g->g_d, s, &n));
+  double* h_out = g->h_stage;
+  double* h_g = g->h_stage + 8;
+  int* h_status = reinterpret_cast<int*>(g->h_stage + 8 + ctx->ntheta + 1);
+  CK(cudaMemcpyAsync(h_out, g->ws.out, sizeof(double) * 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h_g, g->g_d, sizeof(double) * ntheta, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h_status, g->ws.status, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  t_launches = n;
+  if (h_status[2]) return fail(FGPU_ETIMEOUT, "a bounded wait in a kernel gave up");
+  *info = h_status[0];
+  *ll = (*info == 0) ? h_out[0] : std::nan("");
+  for (int k = 0; k < ntheta; ++k) dll[k] = (*info == 0) ? h_g[k] : std::nan("");
+  return 0;
 }
 
 int fgpu_plan_create(fgpu_plan** out, fgpu_ctx* const* ctxs, int nprob, int ldtheta) {

@@ -484,7 +484,8 @@ __global__ void __launch_bounds__(256) k_potf2(const Prob* __restrict__ probs, i
 __global__ void __launch_bounds__(256) k_trsm(const Prob* __restrict__ probs, int step) {
   const Prob& P = probs[blockIdx.y];
   const int ti = step + 1 + blockIdx.x;
-  if (step >= P.nsteps || ti > P.nsteps) return;
+  const int last = P.nrt ? P.nrt - 1 : P.nsteps;  // last 64-row tile
+  if (step >= P.nsteps || ti > last) return;
   if (*(volatile int*)&P.status[1]) return;
   __shared__ double L[TB * (TB + 1)];
   __shared__ double B[TB * (TB + 1)];
@@ -532,7 +533,8 @@ __device__ __forceinline__ void dmma_8x8x4(double& c0, double& c1, double a, dou
 __global__ void __launch_bounds__(128) k_update(const Prob* __restrict__ probs, int step) {
   const Prob& P = probs[blockIdx.z];
   const int ti = step + 1 + blockIdx.x, tj = step + 1 + blockIdx.y;
-  if (step >= P.nsteps || tj >= P.nsteps || ti > P.nsteps || ti < tj) return;
+  const int last = P.nrt ? P.nrt - 1 : P.nsteps;
+  if (step >= P.nsteps || tj >= P.nsteps || ti > last || ti < tj) return;
   if (*(volatile int*)&P.status[1]) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* As = reinterpret_cast<double*>(smem_raw);  // [k][m]
@@ -748,15 +750,20 @@ cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s)
   return cudaGetLastError();
 }
 
-cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s) {
-  const int rows = max_nsteps - step;  // row tiles step+1 .. nsteps (incl. border)
+cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s,
+                        int max_rowtiles) {
+  if (max_rowtiles <= 0) max_rowtiles = max_nsteps + 1;
+  const int rows = max_rowtiles - step - 1;  // row tiles step+1 .. last (incl. border rows)
   if (rows <= 0) return cudaSuccess;
   k_trsm<<<dim3(rows, nprob), 256, 0, s>>>(probs, step);
   return cudaGetLastError();
 }
 
-cudaError_t launch_update(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s) {
+cudaError_t launch_update(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s,
+                          int max_rowtiles) {
+  if (max_rowtiles <= 0) max_rowtiles = max_nsteps + 1;
   const int m = max_nsteps - step - 1;  // trailing column tiles
+  const int mr = max_rowtiles - step - 1;  // trailing row tiles incl. border rows
   if (m <= 0) return cudaSuccess;
   const int smem = 2 * TB * UPD_STRIDE * (int)sizeof(double);
   if (!g_update_attr_set) {
@@ -764,7 +771,7 @@ cudaError_t launch_update(const Prob* probs, int nprob, int step, int max_nsteps
     if (e != cudaSuccess) return e;
     g_update_attr_set = 1;
   }
-  k_update<<<dim3(m + 1, m, nprob), 128, smem, s>>>(probs, step);
+  k_update<<<dim3(mr, m, nprob), 128, smem, s>>>(probs, step);
   return cudaGetLastError();
 }
 

@@ -76,6 +76,11 @@ struct Prob {
   // dot-product kernel build (mode 1): planes scaled by sqrt(l_k) per evaluation
   double* splanes;                // nplanes x Nc
   double* norms;                  // MAX_LEAF x Nc: sum_k u_ik^2 of rbf leaves
+  // FP64 kernels: number of 64-row tiles when extra border rows follow the
+  // right-hand-side tile (the adjoint's identity rows); 0 = nsteps + 1
+  int nrt;
+  double* kinv;                   // adjoint: K^-1 (Nc x Nc, lower)
+  double* gpart;                  // adjoint: per-CTA partial sums
 };
 
 // Encode the two 5-D TMA tensor maps of a problem's digit-plane buffer into
@@ -91,8 +96,11 @@ cudaError_t launch_prep_planes(const Prob* probs, int nprob, int max_nc, cudaStr
 cudaError_t launch_build_dot(const Prob* probs, int nprob, int max_nsteps, int max_nplanes, cudaStream_t s);
 size_t build_dot_smem_bytes(int nplanes);
 cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s);
-cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s);
-cudaError_t launch_update(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s);
+// max_rowtiles: 64-row tiles of the tallest problem (0 = max_nsteps + 1)
+cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s,
+                        int max_rowtiles = 0);
+cudaError_t launch_update(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s,
+                          int max_rowtiles = 0);
 cudaError_t launch_finalize(const Prob* probs, int nprob, cudaStream_t s);
 cudaError_t launch_backsolve(const Prob* probs, int nprob, int max_nsteps, double* alpha_out,
                              cudaStream_t s, long long* nlaunch);
@@ -118,6 +126,14 @@ cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max
 cudaError_t launch_split_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
 cudaError_t launch_gemm_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
 cudaError_t launch_border_half(const Prob* probs, int nprob, int step, cudaStream_t s);
+
+// Adjoint (grad.cu): identity rows below the right-hand-side tile turn into
+// L^-T during the sweep; K^-1 = L^-T (L^-T)^T; fused dK/dtheta pass.
+cudaError_t launch_identity_border(const Prob* p, int nc, cudaStream_t s);
+cudaError_t launch_syrk_inv(const Prob* p, int nsteps, cudaStream_t s);
+cudaError_t enqueue_grad_passes(const Prob* p, int nsteps, int nk, int optimise_noise, double* g_out,
+                                cudaStream_t s, long long* nlaunch);
+constexpr int GRAD_SLOTS = 33;  // parameters per fused pass + noise slot
 
 // api.cu hooks for other translation units.
 int internal_compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>& plane_dim,
