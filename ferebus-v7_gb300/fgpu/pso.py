@@ -1,0 +1,188 @@
+"""Lockstep particle-swarm driver over the batched engine.
+
+Host-side mirror of FEREBUS-v7's global swarm updater
+(src/optimiser/pso/pso.f90:382-472, init_pso 250-368) in which every
+particle of an iteration -- and, for a multi-atom run, every particle of every
+atom's swarm -- is evaluated in ONE batched engine call (``Plan``), instead of
+one OpenMP thread per particle calling the likelihood (pso.f90:419-452).
+
+Per iteration and particle i (pso.f90:419-452):
+    v_i <- w v_i + c1 r1 (pbest_i - x_i) + c2 r2 (gbest - x_i),  x_i <- x_i + v_i
+then the swarm's costs are evaluated together; a particle whose Cholesky
+fails (info != 0) is re-randomised in its search box and re-evaluated
+(get_cost, src/optimiser/pso/particle.f90:149-162) in follow-up batches; then
+personal bests, then the global best in particle order (pso.f90:454-459,
+"<=" comparisons).  The initial swarm is evaluated once without retries
+(init_particle, particle.f90:53-100); a failed initial particle starts with
+cost +inf.  Stopping: a fixed iteration count (optimiser_type.f90:118-133) or
+the relative-change criterion (pso.f90:619-636).
+
+The forced swarm updater (pso.f90:485-558) updates the global best inside the
+particle loop, so its trajectory is inherently sequential; it is not offered
+here.  Random numbers come from numpy's PCG64, not the reference's RNG, so
+trajectories match the reference in distribution, not bit for bit.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .gpr import Plan
+
+
+@dataclass
+class SwarmConfig:
+    """[optimiser.pso] of the reference's TOML (src/config/optimiser/pso/pso.f90)."""
+    swarm_size: int = 50
+    iterations: int = 1000
+    inertia_weight: float = 0.729
+    cognitive_learning_rate: float = 1.494
+    social_learning_rate: float = 1.494
+    stall_iterations: int = 0        # 0: no relative-change stopping
+    tolerance: float = 1e-8
+    max_retries: int = 64            # bound on re-randomisations per particle per iteration
+
+
+@dataclass
+class SwarmState:
+    x: np.ndarray
+    v: np.ndarray
+    cost: np.ndarray
+    pbest_x: np.ndarray
+    pbest_cost: np.ndarray
+    gbest_x: np.ndarray
+    gbest_cost: float
+    lo: np.ndarray
+    hi: np.ndarray
+    history: list = field(default_factory=list)
+    stall_count: int = 0
+    stall_cost: float = np.inf
+    evaluations: int = 0
+    failures: int = 0
+
+
+class LockstepPSO:
+    """One PSO per problem (atom / property); all swarms advance together.
+
+    ``problems`` is a list of ``(engine, search_min, search_max)``; each
+    engine is an ``fgpu.Engine`` (one training set).  Cost = -logL.
+    """
+
+    def __init__(self, problems, config: SwarmConfig, seed=17, evaluate=None):
+        self.cfg = config
+        self.rng = np.random.default_rng(seed)
+        self.engines = [p[0] for p in problems]
+        self.boxes = [(np.asarray(p[1], float), np.asarray(p[2], float)) for p in problems]
+        self.ntheta = [len(b[0]) for b in self.boxes]
+        S = config.swarm_size
+        self.owner = np.repeat(np.arange(len(problems)), S)
+        if evaluate is None:
+            plan = Plan([e for e in self.engines for _ in range(S)], ldtheta=max(self.ntheta))
+            evaluate = plan.run
+            self.plan = plan
+        self.evaluate_batch = evaluate   # list of positions -> (ll, info)
+        self.states = []
+
+    # -- batched cost evaluation with the reference's retry rule -------------
+    def _evaluate(self, positions, retry):
+        """positions: list over all particles (each its problem's ntheta).
+        Returns costs (+inf for particles that failed and were not retried)."""
+        S = self.cfg.swarm_size
+        ll, info = self.evaluate_batch(positions)
+        ll, info = np.asarray(ll, float), np.asarray(info)
+        cost = -ll
+        bad = np.nonzero(info != 0)[0]
+        tries = 0
+        while retry and bad.size and tries < self.cfg.max_retries:
+            tries += 1
+            for k in bad:
+                a = self.owner[k]
+                lo, hi = self.boxes[a]
+                st = self.states[a]
+                i = k - a * S
+                delta = hi - lo
+                st.x[i] = self.rng.uniform(lo, hi)
+                st.v[i] = self.rng.uniform(-delta, delta)
+                positions[k] = st.x[i]
+                st.failures += 1
+            ll, info2 = self.evaluate_batch(positions)
+            mask = np.isin(np.arange(len(cost)), bad)
+            cost = np.where(mask, -np.asarray(ll, float), cost)
+            info = np.where(mask, np.asarray(info2), 0)
+            bad = np.nonzero(info != 0)[0]
+        for k in bad:
+            cost[k] = np.inf
+        for a, st in enumerate(self.states):
+            st.evaluations += S
+        return cost
+
+    def _positions(self):
+        return [st.x[i] for st in self.states for i in range(self.cfg.swarm_size)]
+
+    def initialise(self):
+        """init_pso: uniform positions in the box, velocities in +-(max - min)."""
+        S = self.cfg.swarm_size
+        self.states = []
+        for (lo, hi), n in zip(self.boxes, self.ntheta):
+            delta = hi - lo
+            x = self.rng.uniform(lo, hi, size=(S, n))
+            v = self.rng.uniform(-delta, delta, size=(S, n))
+            self.states.append(SwarmState(x=x, v=v, cost=np.full(S, np.inf), pbest_x=x.copy(),
+                                          pbest_cost=np.full(S, np.inf), gbest_x=x[0].copy(),
+                                          gbest_cost=np.inf, lo=lo, hi=hi))
+        cost = self._evaluate(self._positions(), retry=False)
+        for a, st in enumerate(self.states):
+            c = cost[a * S:(a + 1) * S]
+            st.cost[:] = c
+            st.pbest_cost[:] = c
+            st.pbest_x[:] = st.x
+            for i in range(S):
+                if c[i] <= st.gbest_cost:
+                    st.gbest_cost = c[i]
+                    st.gbest_x = st.x[i].copy()
+            st.history.append(st.gbest_cost)
+
+    def step(self):
+        """One global_swarm_update for every swarm, one batched evaluation."""
+        cfg, S = self.cfg, self.cfg.swarm_size
+        for st in self.states:
+            n = st.x.shape[1]
+            r1 = self.rng.random((S, n))
+            r2 = self.rng.random((S, n))
+            st.v = (cfg.inertia_weight * st.v + cfg.cognitive_learning_rate * r1 * (st.pbest_x - st.x)
+                    + cfg.social_learning_rate * r2 * (st.gbest_x - st.x))
+            st.x = st.x + st.v
+        cost = self._evaluate(self._positions(), retry=True)
+        done = []
+        for a, st in enumerate(self.states):
+            c = cost[a * S:(a + 1) * S]
+            st.cost[:] = c
+            better = c <= st.pbest_cost
+            st.pbest_x[better] = st.x[better]
+            st.pbest_cost[better] = c[better]
+            for i in range(S):
+                if c[i] <= st.gbest_cost:
+                    st.gbest_cost = c[i]
+                    st.gbest_x = st.x[i].copy()
+            st.history.append(st.gbest_cost)
+            done.append(self._stop(st))
+        return all(done)
+
+    def _stop(self, st):
+        """Relative-change stopping criterion (pso.f90:619-636)."""
+        if self.cfg.stall_iterations <= 0:
+            return False
+        if st.stall_cost != 0 and abs((st.gbest_cost - st.stall_cost) / st.stall_cost) <= self.cfg.tolerance:
+            st.stall_count += 1
+        else:
+            st.stall_count = 0
+            st.stall_cost = st.gbest_cost
+        return st.stall_count >= self.cfg.stall_iterations
+
+    def run(self, iterations=None):
+        self.initialise()
+        for _ in range(iterations if iterations is not None else self.cfg.iterations):
+            if self.step():
+                break
+        return [(st.gbest_x, st.gbest_cost) for st in self.states]
