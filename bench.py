@@ -326,9 +326,14 @@ def main():
     fp64_equiv = fp64_flops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
     traffic = None
     tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
+    if mode == "tcgen05" and os.path.exists(tf) and upd_n:
+        # bytes per 128 x 64 tile from one ncu capture, scaled to this run's
+        # tiles per launch (traffic grows with the tiles processed)
         try:
-            traffic = json.load(open(tf)).get(f"k_update_bytes_per_launch_{mode}")
+            per_tile = json.load(open(tf))["k_ozaki_update_bytes_per_tile"]
+            nt = -(-p.N // 128)
+            tiles = sum((nt - s - 1) * (nt - s) for s in range(nt)) * S
+            traffic = per_tile * tiles / upd_n
         except Exception:
             traffic = None
     stage_ms = {k: v[0] for k, v in stages.items() if v[1]}

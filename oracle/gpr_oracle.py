@@ -499,3 +499,84 @@ def cholesky_python(K):
         if j + 1 < n:
             L[j + 1:, j] = (A[j + 1:, j] - L[j + 1:, :j] @ L[j, :j]) / L[j, j]
     return L, 0
+
+
+def loglik_grad_columns(kspec, theta, X, y, mu, likelihood, noise, optimise_noise):
+    """Memory-light FP64 gradient for large N: the same formula as
+    ``loglik_grad`` (1/2 sum_ij W_ij dK_ij/dtheta, W = a a^T / s - K^-1), with
+    dK/dtheta formed one column at a time (rows i >= j, weight 2 off the
+    diagonal) instead of one dense matrix per parameter."""
+    theta = np.asarray(theta, dtype=np.float64)
+    X = np.asarray(X, dtype=np.float64)
+    n, d = X.shape
+    nk = kernel_nparams(kspec)
+    if optimise_noise:
+        noise = float(theta[nk])
+    tens = Tensors(X, lazy=True)
+    res = loglik(kspec, theta, X, y, mu, likelihood, noise, optimise_noise, tens=tens, want=True)
+    if res["info"] != 0:
+        return res["ll"], None, res["info"]
+    L = res["L"]
+    Kinv = lapack.dpotri(L, lower=1)[0]
+    a = res["alpha"]
+    s = 1.0 if likelihood == MARGINAL else res["sigma2"]
+    nodes = parse_kspec(kspec)
+    # leaf parameter offsets and transformed parameters
+    leaves, p = [], 0
+    for node in nodes:
+        if node[0] == "leaf":
+            k = leaf_nparams(node[1], node[2])
+            leaves.append((p, leaf_transform(node[1], theta[p:p + k])))
+            p += k
+    g = np.zeros(len(theta))
+    xt = X.T
+    cyc = np.arange(2, d, 3)
+    for j in range(n):
+        w = a[j:] * a[j] / s - Kinv[j:, j]
+        w[1:] *= 2.0
+        diff = xt[:, j:] - xt[:, j:j + 1]
+        wrapped = diff.copy()
+        c = wrapped[cyc]
+        aa = np.abs(c) + PI
+        wrapped[cyc] = np.where(c == 0.0, 0.0, np.sign(c) * ((aa - np.trunc(aa / TWOPI) * TWOPI) - PI))
+        P = np.sin(np.sqrt(diff * diff) / 2.0) ** 2
+        vals, derivs, li = [], [], 0
+        stack = []
+        for node in nodes:
+            if node[0] == "leaf":
+                op, dims = node[1], node[2]
+                p0, prm = leaves[li]
+                li += 1
+                m = len(w)
+                if op == RBF:
+                    t = prm[:, None] * diff[dims] ** 2
+                    v = np.exp(-0.5 * t.sum(axis=0))
+                    dv = [(p0 + q, v * (-0.5 * t[q])) for q in range(len(dims))]
+                elif op == RBF_CYCLIC:
+                    t = prm[:, None] * wrapped[dims] ** 2
+                    v = np.exp(-0.5 * t.sum(axis=0))
+                    dv = [(p0 + q, v * (-0.5 * t[q])) for q in range(len(dims))]
+                elif op == PERIODIC:
+                    t = prm[:, None] * P[dims]
+                    v = np.exp(-2.0 * t.sum(axis=0))
+                    dv = [(p0 + q, v * (4.0 * t[q])) for q in range(len(dims))]
+                elif op == LINEAR:
+                    v = np.full(m, float(np.sum(1.0 / prm)))
+                    dv = [(p0 + q, np.full(m, 1.0 / prm[q])) for q in range(len(dims))]
+                else:
+                    v = np.full(m, float(prm[0]))
+                    dv = [(p0, np.ones(m))]
+                stack.append((v, dv))
+            else:
+                vb, db = stack.pop()
+                va, da = stack.pop()
+                if node[1] == SUM:
+                    stack.append((va + vb, da + db))
+                else:
+                    stack.append((va * vb, [(q, x * vb) for q, x in da] + [(q, va * x) for q, x in db]))
+        _, dK = stack[0]
+        for q, x in dK:
+            g[q] += 0.5 * float(np.dot(w, x))
+        if optimise_noise:
+            g[nk] += 0.5 * (a[j] * a[j] / s - Kinv[j, j])
+    return res["ll"], g, 0

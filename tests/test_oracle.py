@@ -134,3 +134,14 @@ def test_mean_functions_host_mirror_matches_oracle():
         a = mean_vector(kind, X, y)
         b = O.mean_vector(kind, X, y)
         assert np.allclose(a, b, rtol=1e-10, atol=1e-12), kind
+
+
+@pytest.mark.parametrize("lik", [0, 1])
+def test_columnwise_gradient_matches_dense(lik):
+    X, y = _data(50, 4, 11)
+    ks = [O.RBF, 2, 1, 2, O.PERIODIC, 1, 4, O.PROD, O.CONSTANT, 0, O.SUM, O.LINEAR, 1, 3, O.SUM]
+    th = np.array([0.3, 0.5, 0.2, 0.7, 0.1, 2e-4])
+    mu = O.mean_vector("constant", X, y)
+    _, a, _ = O.loglik_grad(ks, th, X, y, mu, lik, 1e-5, True)
+    _, b, _ = O.loglik_grad_columns(ks, th, X, y, mu, lik, 1e-5, True)
+    assert np.allclose(a, b, rtol=1e-9, atol=1e-12)
