@@ -5,7 +5,9 @@
 // Every kernel takes the device array of problem descriptors and indexes it
 // by blockIdx.z (tile kernels) or blockIdx.x (per-problem kernels), so one
 // launch serves a whole ragged batch.
+#include "../../include/fgpu.h"
 #include "fgpu_internal.h"
+#include "iexp.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -89,7 +91,7 @@ __device__ __forceinline__ double leaf_value(const Leaf& L, const double* __rest
         double dlt = Pi[(p0 + k) * TB + ri] - Pj[(p0 + k) * TB + cj];
         acc = fma(ls[q0 + k], dlt * dlt, acc);
       }
-      return exp(-0.5 * acc);
+      return iexp_neg(-0.5 * acc);
     }
     case L_PERIODIC: {
       // periodic_kernel.f90:181-206 on distance_matrix.f90:130-142:
@@ -102,7 +104,7 @@ __device__ __forceinline__ double leaf_value(const Leaf& L, const double* __rest
         double t = fma(si, cjv, -(ci * sj));
         acc = fma(ls[q0 + k], t * t, acc);
       }
-      return exp(-2.0 * acc);
+      return iexp_neg(-2.0 * acc);
     }
     case L_RBF_CYCLIC: {
       // stationary_cyclic_kernel.f90:104-127 on distance_matrix.f90:95-128:
@@ -116,7 +118,7 @@ __device__ __forceinline__ double leaf_value(const Leaf& L, const double* __rest
         }
         acc = fma(ls[q0 + k], dlt * dlt, acc);
       }
-      return exp(-0.5 * acc);
+      return iexp_neg(-0.5 * acc);
     }
     case L_LINEAR:
       // linear_kernel.f90:70-76 with the reference's default order 0:
@@ -384,12 +386,12 @@ __global__ void __launch_bounds__(256) k_build_dot(const Prob* __restrict__ prob
                 double dot = 0.0;
                 for (int k = 0; k < L.n; ++k) dot = fma(Pi[(L.plane0 + k) * TB + r], Pj[(L.plane0 + k) * TB + c], dot);
                 const double e = (i == j) ? 0.0 : (Ni[tok * TB + r] + Nj[tok * TB + c]) - 2.0 * dot;
-                lv = exp(-0.5 * e);
+                lv = iexp_neg(-0.5 * e);
               } else if (L.type == L_PERIODIC) {
                 double dot = 0.0;
                 for (int k = 0; k < 2 * L.n; ++k)
                   dot = fma(Pi[(L.plane0 + k) * TB + r], Pj[(L.plane0 + k) * TB + c], dot);
-                lv = (i == j) ? 1.0 : exp(dot - leaf_c[tok]);
+                lv = (i == j) ? 1.0 : iexp_neg(dot - leaf_c[tok]);
               } else {
                 lv = leaf_value(L, Pi, Pj, r, c, ls, sp.cyclic, leaf_c[tok]);
               }
@@ -794,3 +796,32 @@ cudaError_t launch_backsolve(const Prob* probs, int nprob, int max_nsteps, doubl
 }
 
 }  // namespace fgpu
+
+// ---------------------------------------------------------------------------
+// diagnostic: the device exponential of the kernel-matrix builds on host values
+// ---------------------------------------------------------------------------
+namespace fgpu {
+__global__ void k_diag_exp(const double* __restrict__ x, double* __restrict__ y, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = iexp_neg(x[i]);
+}
+}  // namespace fgpu
+
+extern "C" int fgpu_diag_exp(const double* x, double* y, int n) {
+  using namespace fgpu;
+  internal_clear_error();
+  if (n < 0 || (n > 0 && (!x || !y))) return internal_fail(FGPU_EINVAL, "fgpu_diag_exp: bad arguments");
+  if (n == 0) return FGPU_OK;
+  double* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(double) * 2 * (size_t)n);
+  if (e != cudaSuccess) return internal_fail(FGPU_ENOMEM, cudaGetErrorString(e));
+  if ((e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice)) == cudaSuccess) {
+    k_diag_exp<<<(n + 255) / 256, 256>>>(d, d + n, n);
+    internal_add_launches(1);
+    if ((e = cudaGetLastError()) == cudaSuccess)
+      e = cudaMemcpy(y, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(d);
+  if (e != cudaSuccess) return internal_fail(FGPU_ECUDA, cudaGetErrorString(e));
+  return FGPU_OK;
+}

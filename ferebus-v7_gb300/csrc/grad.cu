@@ -10,6 +10,7 @@
 // leaf values and their per-feature factors from the feature planes tile by
 // tile, exactly as the kernel-matrix build does.
 #include "fgpu_internal.h"
+#include "iexp.cuh"
 
 #include <cmath>
 
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(256) k_grad(const Prob* __restrict__ pp, int q
                 }
                 e = fma(ls[L.param0 + k], d * d, e);
               }
-              v = exp(-0.5 * e);
+              v = iexp_neg(-0.5 * e);
             } else if (L.type == L_PERIODIC) {
               for (int k = 0; k < L.n; ++k) {
                 const double si = X[(size_t)(L.plane0 + 2 * k) * nc + i], ci = X[(size_t)(L.plane0 + 2 * k + 1) * nc + i];
@@ -154,7 +155,7 @@ __global__ void __launch_bounds__(256) k_grad(const Prob* __restrict__ pp, int q
                 const double tt = fma(si, cj, -(ci * sj));
                 e = fma(ls[L.param0 + k], tt * tt, e);
               }
-              v = exp(-2.0 * e);
+              v = iexp_neg(-2.0 * e);
             } else if (L.type == L_LINEAR) {
               v = 0.0;
               for (int k = 0; k < L.n; ++k) v += 1.0 / ls[L.param0 + k];

@@ -60,6 +60,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+// one non-blocking probe of an mbarrier phase
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(su32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // tcgen05 shared-memory descriptor, no swizzle, K-major core matrices
 // (8 rows x 16 bytes): lbo = byte stride between core matrices along K,
 // sbo = along M/N; descriptor version 1 (bits 46-47).
@@ -314,11 +325,13 @@ __global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, i
 // (prefix table from the host), column tile major, row tile minor.
 // ---------------------------------------------------------------------------
 constexpr int CH = 8;                                // k-chunks of 16 per 128-panel (one MMA each)
-constexpr int NSTAGE = 5;
+constexpr int NSTAGE = 3;
 constexpr uint32_t A_STAGE = NSLICE * 4096;          // 7 planes x 2 k-groups x 128 rows x 16 B
 constexpr uint32_t B_STAGE = NSLICE * 2048;          // 7 planes x 2 k-groups x 64 rows x 16 B
 constexpr uint32_t STAGE = A_STAGE + B_STAGE;        // 43008 B
-constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + 256;
+constexpr uint32_t ACC_HI_TILE = 128 * 64 * 8;       // accumulator tile, high words (64 KB)
+constexpr uint32_t ACC_LO_TILE = 128 * 64 * 4;       // low 24-bit words (32 KB)
+constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + ACC_HI_TILE + ACC_LO_TILE + 256;
 constexpr int UPD_THREADS = 320;
 
 __device__ __forceinline__ void tma_load_5d(void* dst, const void* tmap, int c0, int c1, int c2, int c3, int c4,
@@ -327,6 +340,12 @@ __device__ __forceinline__ void tma_load_5d(void* dst, const void* tmap, int c0,
       "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
       "%6}], [%7];" ::"r"(su32(dst)),
       "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(su32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(su32(dst)),
+      "l"(src), "r"(bytes), "r"(su32(bar))
       : "memory");
 }
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
@@ -361,11 +380,15 @@ __device__ __forceinline__ bool decode_tile(const Prob* __restrict__ probs, cons
 __global__ void __launch_bounds__(UPD_THREADS, 1)
     k_ozaki_update(const Prob* __restrict__ probs, int nprob, int s, const int* __restrict__ prefix) {
   extern __shared__ __align__(1024) unsigned char smu[];
-  uint64_t* full = reinterpret_cast<uint64_t*>(smu + NSTAGE * STAGE);
+  long long* hi_s = reinterpret_cast<long long*>(smu + NSTAGE * STAGE);
+  int* lo_s = reinterpret_cast<int*>(smu + NSTAGE * STAGE + ACC_HI_TILE);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smu + NSTAGE * STAGE + ACC_HI_TILE + ACC_LO_TILE);
   uint64_t* empty = full + NSTAGE;
   uint64_t* tfull = full + 2 * NSTAGE;
   uint64_t* tempty = tfull + 1;
-  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 2);
+  uint64_t* afull = tfull + 2;   // accumulator tile landed in shared memory
+  uint64_t* aempty = tfull + 3;  // epilogue done with the accumulator tile
+  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 4);
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
@@ -376,6 +399,8 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
     }
     mbar_init(tfull, 1);
     mbar_init(tempty, 256);
+    mbar_init(afull, 1);
+    mbar_init(aempty, 256);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 9) {
@@ -391,7 +416,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
   if (warp == 8) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
-      uint32_t g = 0;
+      uint32_t g = 0, it = 0;
       for (int t = blockIdx.x; t < total; t += gridDim.x) {
         int p, ti, tj;
         decode_tile(probs, prefix, nprob, s, t, p, ti, tj);
@@ -399,7 +424,20 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
         if (P.status[1]) continue;
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_b) : "memory");
+        // The accumulator tile goes into its shared buffer as soon as the
+        // previous tile's epilogue has released it (polled between operand
+        // chunks, so the chunk loads never wait for the epilogue); step 0
+        // writes the accumulators without reading them.
+        bool acc_issued = (s == 0);
+        const size_t tile = (size_t)(tj * P.nt128 + ti) * (128 * 64);
+        const uint32_t apar = (it & 1) ^ 1;
         for (int c = 0; c < CH; ++c, ++g) {
+          if (!acc_issued && mbar_test(aempty, apar)) {
+            mbar_expect_tx(afull, ACC_HI_TILE + ACC_LO_TILE);
+            bulk_g2s(hi_s, P.acc_hi + tile, ACC_HI_TILE, afull);
+            bulk_g2s(lo_s, P.acc_lo + tile, ACC_LO_TILE, afull);
+            acc_issued = true;
+          }
           const int st = g % NSTAGE;
           if (!mbar_wait(&empty[st], ((g / NSTAGE) & 1) ^ 1)) {
             s_abort = 1;
@@ -411,6 +449,16 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
           tma_load_5d(As + A_STAGE, P.tmap_b, 0, (tj & 1) * 2, 2 * c, 0, tj >> 1, &full[st]);
         }
         if (s_abort) break;
+        if (!acc_issued) {
+          if (!mbar_wait(aempty, apar)) {
+            s_abort = 1;
+            break;
+          }
+          mbar_expect_tx(afull, ACC_HI_TILE + ACC_LO_TILE);
+          bulk_g2s(hi_s, P.acc_hi + tile, ACC_HI_TILE, afull);
+          bulk_g2s(lo_s, P.acc_lo + tile, ACC_LO_TILE, afull);
+        }
+        ++it;
       }
     }
   } else if (warp == 9) {
@@ -499,38 +547,30 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
       // TMEM drained: let the next tile's MMAs start
       asm volatile("tcgen05.fence::before_thread_sync;");
       mbar_arrive(tempty);
-      ++it;
       const size_t tile = (size_t)(tj * P.nt128 + ti) * (128 * 64);
       long long* gh = P.acc_hi + tile;
       int* gl = P.acc_lo + tile;
       const bool first = (s == 0);
-#pragma unroll
-      for (int gq = 0; gq < 4; ++gq) {
-        long long ah[8];
-        int al[8];
-        if (!first) {
-#pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            const int idx = (h * 32 + gq * 8 + jj) * 128 + r;
-            ah[jj] = gh[idx];
-            al[jj] = gl[idx];
-          }
-        }
-#pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          const int idx = (h * 32 + gq * 8 + jj) * 128 + r;
-          long long hi = hv[gq * 8 + jj];
-          long long lo = lv[gq * 8 + jj];
-          if (!first) {
-            hi += ah[jj];
-            lo += al[jj];
-            hi += lo >> 24;
-            lo &= 0xFFFFFF;
-          }
-          gh[idx] = hi;
-          gl[idx] = (int)lo;
-        }
+      if (!first && !mbar_wait(afull, it & 1)) {
+        s_abort = 1;
+        break;
       }
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int idx = (h * 32 + q) * 128 + r;
+        long long hi = hv[q];
+        long long lo = lv[q];
+        if (!first) {
+          hi += hi_s[idx];
+          lo += lo_s[idx];
+          hi += lo >> 24;
+          lo &= 0xFFFFFF;
+        }
+        gh[idx] = hi;
+        gl[idx] = (int)lo;
+      }
+      if (!first) mbar_arrive(aempty);
+      ++it;
     }
   }
   __syncthreads();

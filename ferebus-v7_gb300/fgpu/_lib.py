@@ -19,7 +19,7 @@ EXPORTS = (
     "fgpu_plan_create", "fgpu_plan_run_device", "fgpu_plan_run", "fgpu_plan_destroy",
     "fgpu_destroy", "fgpu_last_error", "fgpu_version", "fgpu_last_launch_count",
     "fgpu_plan_set_profiling", "fgpu_plan_stage_times", "fgpu_loglik_noalloc",
-    "fgpu_set_trailing_update",
+    "fgpu_set_trailing_update", "fgpu_diag_exp",
 )
 
 c_double_p = C.POINTER(C.c_double)
@@ -80,6 +80,8 @@ def load(path=None):
     lib.fgpu_loglik_noalloc.restype = C.c_int
     lib.fgpu_set_trailing_update.argtypes = [C.c_int]
     lib.fgpu_set_trailing_update.restype = C.c_int
+    lib.fgpu_diag_exp.argtypes = [c_double_p, c_double_p, C.c_int]
+    lib.fgpu_diag_exp.restype = C.c_int
     _lib = lib
     return lib
 

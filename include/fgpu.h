@@ -158,6 +158,12 @@ int fgpu_loglik_noalloc(int N, int d, const double* X_dev, const double* y_dev, 
 int fgpu_plan_set_profiling(fgpu_plan* plan, int enable);
 int fgpu_plan_stage_times(fgpu_plan* plan, double* ms, int* count);
 
+/* The device exponential every kernel-matrix entry goes through (a
+ * fixed-point evaluation on the integer pipes), applied to n host values:
+ * y[i] = exp(x[i]).  Diagnostic only, for checking it against the host libm;
+ * synchronous.  The reference has no counterpart. */
+int fgpu_diag_exp(const double* x, double* y, int n);
+
 /* Thread-local message for the last failing call on this thread. */
 const char* fgpu_last_error(void);
 
