@@ -415,46 +415,89 @@ __global__ void __launch_bounds__(256) k_build_dot(const Prob* __restrict__ prob
 }
 
 // ---------------------------------------------------------------------------
-// diagonal block factorisation (unblocked, right-looking) + log-det partial
+// diagonal block factorisation (blocked, left-looking) + log-det partial
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_potf2(const Prob* __restrict__ probs, int step) {
+  // Blocked left-looking factorisation of the 64 x 64 diagonal block in
+  // shared memory, panels of 8 columns (the dot-product order of LAPACK's
+  // dpotf2, lapack/dpotf2.f): (a) the panel minus the finished columns times
+  // their rows, all threads; (b) the 8 x 8 diagonal block by one warp in
+  // registers (shuffles, no block barriers); (c) the rows below by forward
+  // substitution, one thread per row.  Three block barriers per panel.
   const Prob& P = probs[blockIdx.x];
   if (step >= P.nsteps) return;
   if (*(volatile int*)&P.status[1]) return;
-  __shared__ double A[TB * (TB + 1)];
-  __shared__ double rdiag;
+  constexpr int LDA = TB + 1;
+  __shared__ double A[TB * LDA];  // A[c * LDA + r]
+  __shared__ double rdg[TB];      // 1 / L_cc
   __shared__ int fail_col;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const size_t ld = (size_t)P.ld;
   double* Kd = P.K + (size_t)(step * TB) * ld + step * TB;
   for (int e = tid; e < TB * TB; e += blockDim.x) {
     const int r = e % TB, c = e / TB;
-    A[c * (TB + 1) + r] = Kd[(size_t)c * ld + r];
+    A[c * LDA + r] = Kd[(size_t)c * ld + r];
   }
   if (tid == 0) fail_col = -1;
   __syncthreads();
-  for (int j = 0; j < TB; ++j) {
-    if (tid == 0) {
-      const double d = A[j * (TB + 1) + j];
-      if (!(d > 0.0)) {
-        fail_col = j;
-      } else {
-        const double s = sqrt(d);
-        A[j * (TB + 1) + j] = s;
-        rdiag = 1.0 / s;
+  for (int c0 = 0; c0 < TB; c0 += 8) {
+    // (a) columns c0..c0+7, rows >= column: subtract sum_{k < c0} L_rk L_ck
+    if (c0 > 0) {
+      const int r = tid & (TB - 1), cp = c0 + 2 * (tid >> 6);
+      if (r >= cp) {
+        double a0 = A[cp * LDA + r], a1 = A[(cp + 1) * LDA + r];
+        for (int k = 0; k < c0; ++k) {
+          const double l = A[k * LDA + r];
+          a0 = fma(-l, A[k * LDA + cp], a0);
+          a1 = fma(-l, A[k * LDA + cp + 1], a1);
+        }
+        A[cp * LDA + r] = a0;
+        if (r > cp) A[(cp + 1) * LDA + r] = a1;
+      }
+    }
+    __syncthreads();
+    // (b) 8 x 8 diagonal block: lane i < 8 holds row c0 + i
+    if (warp == 0) {
+      double v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = (lane < 8 && k <= lane) ? A[(c0 + k) * LDA + c0 + lane] : 0.0;
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) {
+        const double d = __shfl_sync(0xffffffffu, v[jj], jj);
+        if (!(d > 0.0)) {  // d is the same in every lane: the warp leaves together
+          if (lane == 0) fail_col = c0 + jj;
+          break;
+        }
+        const double sd = sqrt(d);
+        const double rd = 1.0 / sd;
+        if (lane == jj) v[jj] = sd;
+        if (lane > jj) v[jj] *= rd;
+#pragma unroll
+        for (int c = jj + 1; c < 8; ++c) {
+          const double lcj = __shfl_sync(0xffffffffu, v[jj], c);
+          if (lane >= c) v[c] = fma(-v[jj], lcj, v[c]);
+        }
+        if (lane == 0) rdg[c0 + jj] = rd;
+      }
+      if (lane < 8) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (k <= lane) A[(c0 + k) * LDA + c0 + lane] = v[k];
       }
     }
     __syncthreads();
     if (fail_col >= 0) break;
-    if (tid > j && tid < TB) A[j * (TB + 1) + tid] *= rdiag;
-    __syncthreads();
-    // rank-1 update: thread (row r, group g) updates columns j+1+g, +4, ... <= r
-    {
-      const int r = tid & (TB - 1), g = tid >> 6;
-      if (r > j) {
-        const double ljr = A[j * (TB + 1) + r];
-        for (int c = j + 1 + g; c <= r; c += 4)
-          A[c * (TB + 1) + r] = fma(-ljr, A[j * (TB + 1) + c], A[c * (TB + 1) + r]);
+    // (c) rows below the diagonal block: forward substitution over the panel
+    if (tid < TB - c0 - 8) {
+      const int r = c0 + 8 + tid;
+      double x[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        double a = A[(c0 + c) * LDA + r];
+#pragma unroll
+        for (int k = 0; k < c; ++k) a = fma(-x[k], A[(c0 + k) * LDA + c0 + c], a);
+        x[c] = a * rdg[c0 + c];
+        A[(c0 + c) * LDA + r] = x[c];
       }
     }
     __syncthreads();
@@ -468,14 +511,14 @@ __global__ void __launch_bounds__(256) k_potf2(const Prob* __restrict__ probs, i
   }
   for (int e = tid; e < TB * TB; e += blockDim.x) {
     const int r = e % TB, c = e / TB;
-    if (r >= c) Kd[(size_t)c * ld + r] = A[c * (TB + 1) + r];
+    if (r >= c) Kd[(size_t)c * ld + r] = A[c * LDA + r];
   }
   // log-det partial: 2 * sum log(L_jj) is formed in the epilogue
   // (arith.f90:72-93); here the block's sum of logs, in column order.
   if (tid < 32) {
-    double s = log(A[(2 * tid) * (TB + 1) + 2 * tid]) + log(A[(2 * tid + 1) * (TB + 1) + 2 * tid + 1]);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (tid == 0) P.logdet_part[step] = s;
+    double sl = log(A[(2 * tid) * LDA + 2 * tid]) + log(A[(2 * tid + 1) * LDA + 2 * tid + 1]);
+    for (int o = 16; o > 0; o >>= 1) sl += __shfl_down_sync(0xffffffffu, sl, o);
+    if (tid == 0) P.logdet_part[step] = sl;
   }
 }
 
