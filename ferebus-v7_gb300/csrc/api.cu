@@ -106,6 +106,36 @@ int compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>
   return 0;
 }
 
+// Tensor-core build eligibility (tensor-core mode): every leaf rbf, periodic,
+// linear or constant; one or two rbf / periodic leaves whose feature columns,
+// each rounded up to 16, fit the 128 digit columns of the panel buffer.  The
+// environment variable FGPU_BUILD=fp64 keeps the FP64 dot-product build.
+void plan_tc_build(Spec& sp) {
+  sp.tc_build = 0;
+  sp.ndot = 0;
+  const char* v = getenv("FGPU_BUILD");
+  if (v && (strcmp(v, "fp64") == 0 || strcmp(v, "0") == 0)) return;
+  int koff = 0;
+  for (int l = 0; l < sp.nleaf; ++l) {
+    const Leaf& L = sp.leaf[l];
+    if (L.type == FGPU_RBF_CYCLIC) return;
+    if (L.type != FGPU_RBF && L.type != FGPU_PERIODIC) continue;
+    if (sp.ndot == 2) return;
+    const int nf = L.type == FGPU_PERIODIC ? 2 * L.n : L.n;
+    const int k16 = round_up(nf, 16);
+    if (koff + k16 > NB) return;
+    int lg = 0;
+    while ((1 << lg) < nf) ++lg;  // ceil(log2 nf)
+    sp.dot_leaf[sp.ndot] = l;
+    sp.dot_koff[sp.ndot] = koff;
+    sp.dot_kch[sp.ndot] = k16 / 16;
+    sp.dot_u[sp.ndot] = 60 - lg;
+    koff += k16;
+    sp.ndot++;
+  }
+  sp.tc_build = sp.ndot > 0 ? 1 : 0;
+}
+
 // Per-step tile tables of the persistent tensor-core update: for step s,
 // prefix[s * (nprob + 1) + p] = tiles of problems < p.
 struct UpdSched {
@@ -113,6 +143,8 @@ struct UpdSched {
   std::vector<int> totals;  // tiles per step
   int stride = 0;           // nprob + 1
   int num_sms = 0;
+  int* build_prefix_dev = nullptr;  // nprob + 1: tiles of the tensor-core build
+  int build_total = 0;
 };
 
 struct Workspace {
@@ -130,6 +162,9 @@ struct Workspace {
   unsigned char* tmaps = nullptr;  // 2 x 128 B TMA tensor maps over slices
   double* splanes = nullptr;       // theta-scaled planes (dot-product build)
   double* norms = nullptr;
+  long long* fnorm = nullptr;      // tensor-core build: W_ii of the distance leaves
+  double* fcoef = nullptr;         // tensor-core build: expression coefficients
+  int* fscale = nullptr;           // tensor-core build: leaf scales
 };
 
 // Process-wide default trailing-update mode for contexts created from now on:
@@ -198,6 +233,7 @@ struct fgpu_ctx {
   Spec spec{};
   Spec* spec_d = nullptr;
   double* planes_d = nullptr;
+  double* plane_max_d = nullptr;  // nplanes: max_i |planes[p][i]| (tensor-core build scales)
   double* y_d = nullptr;
   double* mu_d = nullptr;
   std::mutex mu;
@@ -261,9 +297,14 @@ void fill_prob(Prob& p, const fgpu_ctx* c, const double* theta_d, const Workspac
   p.tmap_b = ws.tmaps ? ws.tmaps + 128 : nullptr;
   p.splanes = ws.splanes;
   p.norms = ws.norms;
+  p.plane_max = c->plane_max_d;
+  p.fnorm = ws.fnorm;
+  p.fcoef = ws.fcoef;
+  p.fscale = ws.fscale;
 }
 
-int build_sched(const std::vector<int>& nt128, UpdSched& u, std::vector<void*>* track) {
+int build_sched(const std::vector<int>& nt128, const std::vector<int>& tc_build, UpdSched& u,
+                std::vector<void*>* track) {
   const int nprob = (int)nt128.size();
   int ntmax = 0;
   for (int v : nt128) ntmax = std::max(ntmax, v);
@@ -286,6 +327,13 @@ int build_sched(const std::vector<int>& nt128, UpdSched& u, std::vector<void*>* 
   CK(cudaMalloc(&u.prefix_dev, sizeof(int) * h.size()));
   if (track) track->push_back(u.prefix_dev);
   CK(cudaMemcpy(u.prefix_dev, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
+  // tensor-core build: the whole lower triangle, nt128 (nt128 + 1) tiles of 128 x 64
+  std::vector<int> b(nprob + 1, 0);
+  for (int p = 0; p < nprob; ++p) b[p + 1] = b[p] + (tc_build[p] ? nt128[p] * (nt128[p] + 1) : 0);
+  u.build_total = b[nprob];
+  CK(cudaMalloc(&u.build_prefix_dev, sizeof(int) * b.size()));
+  if (track) track->push_back(u.build_prefix_dev);
+  CK(cudaMemcpy(u.build_prefix_dev, b.data(), sizeof(int) * b.size(), cudaMemcpyHostToDevice));
   return 0;
 }
 
@@ -320,7 +368,12 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
     // 128-wide panels; max_nsteps counts 64-column tiles
     const int nt = max_nsteps / 2, max_nc = max_nsteps * TB;
     STAGE(0, launch_prep_planes(probs_d, nprob, max_nc, s));
+    if (us->build_total > 0) STAGE(0, launch_feat_digits(probs_d, nprob, nt, s));
+    // FP64 dot-product build: every tile of the other problems, the
+    // right-hand-side rows of all
     STAGE(0, launch_build_dot(probs_d, nprob, max_nsteps, max_nplanes, s));
+    if (us->build_total > 0)
+      STAGE(0, launch_build_tc(probs_d, nprob, us->build_prefix_dev, us->build_total, us->num_sms, s));
     STAGE(0, launch_scales(probs_d, nprob, max_nc, s));
     for (int step = 0; step < nt; ++step) {
       if (step > 0) STAGE(5, launch_panel_prep(probs_d, nprob, step, max_nc, s));
@@ -391,6 +444,9 @@ int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track)
     CK(cudaMalloc(&ws.splanes, sizeof(double) * (size_t)std::max(c->spec.nplanes, 1) * nc));
     CK(cudaMalloc(&ws.norms, sizeof(double) * (size_t)MAX_LEAF * nc));
     CK(cudaMemset(ws.norms, 0, sizeof(double) * (size_t)MAX_LEAF * nc));
+    CK(cudaMalloc(&ws.fnorm, sizeof(long long) * 2 * nc));
+    CK(cudaMalloc(&ws.fcoef, sizeof(double) * 4));
+    CK(cudaMalloc(&ws.fscale, sizeof(int) * 2));
     CK(cudaMalloc(&ws.tmaps, 256));
     alignas(64) unsigned char maps[256];
     const int er = encode_slice_maps(maps, ws.slices, c->nt128);
@@ -400,7 +456,7 @@ int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track)
   if (track) {
     for (void* q : {(void*)ws.K, (void*)ws.logdet_part, (void*)ws.out, (void*)ws.z, (void*)ws.escale,
                     (void*)ws.pw2, (void*)ws.acc_hi, (void*)ws.acc_lo, (void*)ws.slices, (void*)ws.tmaps,
-                    (void*)ws.splanes, (void*)ws.norms})
+                    (void*)ws.splanes, (void*)ws.norms, (void*)ws.fnorm, (void*)ws.fcoef, (void*)ws.fscale})
       if (q) track->push_back(q);
   }
   return 0;
@@ -422,9 +478,13 @@ void free_worker(Worker* w) {
   cudaFree(w->ws.tmaps);
   cudaFree(w->ws.splanes);
   cudaFree(w->ws.norms);
+  cudaFree(w->ws.fnorm);
+  cudaFree(w->ws.fcoef);
+  cudaFree(w->ws.fscale);
   cudaFree(w->theta_d);
   cudaFree(w->prob_d);
   cudaFree(w->sched.prefix_dev);
+  cudaFree(w->sched.build_prefix_dev);
   if (w->h_stage) cudaFreeHost(w->h_stage);
   if (w->stream) cudaStreamDestroy(w->stream);
   delete w;
@@ -452,7 +512,9 @@ int make_worker(fgpu_ctx* c, Worker** out) {
   fill_prob(p, c, w->theta_d, w->ws);
   if (cudaMemcpy(w->prob_d, &p, sizeof(Prob), cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(FGPU_ECUDA, "desc copy"));
-  if (c->mode == 1 && (rc = build_sched(std::vector<int>{c->nt128}, w->sched, nullptr)) != 0) return bail(rc);
+  if (c->mode == 1 &&
+      (rc = build_sched(std::vector<int>{c->nt128}, std::vector<int>{c->spec.tc_build}, w->sched, nullptr)) != 0)
+    return bail(rc);
   if ((rc = capture(w->stream, &w->graph, w->prob_d, 1, c->nsteps, c->spec.nplanes, w->ws.status,
                     sizeof(int) * 4, &w->graph_kernels, nullptr, c->mode, &w->sched)) != 0)
     return bail(rc);
@@ -515,6 +577,7 @@ int fgpu_create(fgpu_ctx** out, int N, int d, const double* X, const double* y, 
   c->N = N;
   c->d = d;
   c->mode = default_mode();
+  if (c->mode == 1) plan_tc_build(c->spec);
   c->Nc = round_up(N, c->mode == 1 ? NB : TB);
   c->nt128 = c->Nc / NB;
   c->ld = c->Nc + TB;
@@ -568,6 +631,13 @@ int fgpu_create(fgpu_ctx** out, int N, int d, const double* X, const double* y, 
   }
   CK(cudaMalloc(&c->planes_d, planes.size() * sizeof(double)));
   CK(cudaMemcpy(c->planes_d, planes.data(), planes.size() * sizeof(double), cudaMemcpyHostToDevice));
+  {
+    std::vector<double> pmax(std::max(np, 1), 0.0);
+    for (int p = 0; p < np; ++p)
+      for (int i = 0; i < N; ++i) pmax[p] = std::max(pmax[p], std::fabs(planes[(size_t)p * c->Nc + i]));
+    CK(cudaMalloc(&c->plane_max_d, pmax.size() * sizeof(double)));
+    CK(cudaMemcpy(c->plane_max_d, pmax.data(), pmax.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
   // FP64-mode planes for the adjoint (64-padded), whatever the context's mode
   {
     const int nc64 = round_up(N, TB);
@@ -633,6 +703,7 @@ void fgpu_destroy(fgpu_ctx* ctx) {
   }
   cudaFree(ctx->planes64_d);
   cudaFree(ctx->planes_d);
+  cudaFree(ctx->plane_max_d);
   cudaFree(ctx->y_d);
   cudaFree(ctx->mu_d);
   cudaFree(ctx->spec_d);
@@ -831,9 +902,12 @@ int fgpu_plan_create(fgpu_plan** out, fgpu_ctx* const* ctxs, int nprob, int ldth
   CK(cudaMemcpy(p->probs_d, p->probs_h.data(), sizeof(Prob) * nprob, cudaMemcpyHostToDevice));
   p->mode = ctxs[0]->mode;
   if (p->mode == 1) {
-    std::vector<int> nts;
-    for (int i = 0; i < nprob; ++i) nts.push_back(ctxs[i]->nt128);
-    int rs = build_sched(nts, p->sched, &p->allocations);
+    std::vector<int> nts, tcs;
+    for (int i = 0; i < nprob; ++i) {
+      nts.push_back(ctxs[i]->nt128);
+      tcs.push_back(ctxs[i]->spec.tc_build);
+    }
+    int rs = build_sched(nts, tcs, p->sched, &p->allocations);
     if (rs) {
       fgpu_plan_destroy(p.release());
       return rs;

@@ -300,8 +300,9 @@ __global__ void __launch_bounds__(256) k_build_dot(const Prob* __restrict__ prob
   const Prob& P = probs[blockIdx.z];
   const int ti = blockIdx.x, tj = blockIdx.y;
   if (P.mode != 1 || tj >= P.nsteps || ti > P.nsteps || ti < tj) return;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
   const Spec& sp = *P.spec;
+  if (sp.tc_build && ti != P.nsteps) return;  // built on the tensor cores; only its RHS rows here
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   const int np = sp.nplanes;
   const int nl = sp.nleaf;
   double* Pi = reinterpret_cast<double*>(smem_raw);      // np x 64 planes, row points

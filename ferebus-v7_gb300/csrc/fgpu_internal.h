@@ -45,6 +45,14 @@ struct Spec {
   int nplanes;
   int nkparams;
   uint8_t cyclic[MAX_PLANES];     // rbf-cyclic: plane's feature index is 3, 6, 9, ... (1-based)
+  // tensor-core build (tensor-core mode; leaves rbf / periodic / linear /
+  // constant, at most 2 rbf or periodic "distance" leaves, <= 128 digit columns)
+  int tc_build;
+  int ndot;                       // distance leaves
+  int dot_leaf[2];                // their leaf indices
+  int dot_koff[2];                // first digit column (multiple of 16)
+  int dot_kch[2];                 // k chunks of 16
+  int dot_u[2];                   // W units: <f_i, f_j> 2^(u - 2 - 2s)
 };
 
 // Per-problem descriptor, resident in device memory.
@@ -81,6 +89,11 @@ struct Prob {
   int nrt;
   double* kinv;                   // adjoint: K^-1 (Nc x Nc, lower)
   double* gpart;                  // adjoint: per-CTA partial sums
+  // tensor-core build
+  const double* plane_max;        // nplanes: max_i |planes[p][i]|
+  long long* fnorm;               // 2 x Nc: W_ii of the distance leaves
+  double* fcoef;                  // 4: k = a + b v0 + c v1 + d v0 v1
+  int* fscale;                    // 2: s of the distance leaves, max |f| < 2^s
 };
 
 // Encode the two 5-D TMA tensor maps of a problem's digit-plane buffer into
@@ -126,6 +139,13 @@ cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max
 cudaError_t launch_split_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
 cudaError_t launch_gemm_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
 cudaError_t launch_border_half(const Prob* probs, int nprob, int step, cudaStream_t s);
+
+// Tensor-core kernel-matrix build (build_tc.cu): feature digit planes and
+// exact self products, then the persistent build of the lower triangle.
+// prefix: nprob + 1 tile offsets (nt128 (nt128 + 1) tiles per eligible problem).
+cudaError_t launch_feat_digits(const Prob* probs, int nprob, int max_nt128, cudaStream_t s);
+cudaError_t launch_build_tc(const Prob* probs, int nprob, const int* prefix, int total_tiles, int num_sms,
+                            cudaStream_t s);
 
 // Adjoint (grad.cu): identity rows below the right-hand-side tile turn into
 // L^-T during the sweep; K^-1 = L^-T (L^-T)^T; fused dK/dtheta pass.

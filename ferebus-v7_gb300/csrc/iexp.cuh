@@ -1,29 +1,25 @@
-// exp(x) for the kernel-matrix entries, evaluated on the integer pipes so
-// that it does not compete with the FP64 dot products for the (narrow) FP64
-// pipe of this part.
+// exp(x), x <= 0, for the kernel-matrix entries, evaluated on the integer
+// pipes so that it does not compete with the FP64 work for this part's
+// narrow FP64 pipe.
 //
 //   |y| = |x| log2(e) as a fixed-point number with 64 fractional bits
-//         (53 x 128-bit product, exact to 2^-64),
+//         (64 x 128-bit product, exact to 2^-64),
 //   2^-|y| = 2^-m 2^(j/256) exp(s ln2),  m = ceil(|y|), m - |y| = j/256 + s,
 //   exp(t), 0 <= t < ln2/256: degree-5 Taylor polynomial in 64-bit fixed
 //   point (scale 2^63, truncation below 2^-60), then one round-to-nearest
 //   into the double (subnormals included).
 // Error below 0.51 ulp; measured: never more than 1 ulp from the host libm
-// over 16.7M arguments spanning [-745.2, 0].  x > 0 (only from rounding in
-// the callers' distance forms) goes to the library exp.
+// over 16.7M arguments spanning [-745.2, 0].  Two entries: a double argument
+// (iexp_neg), and an exact fixed-point argument x = -E 2^e (iexp_fixed),
+// which the tensor-core build uses without forming a double.
 #pragma once
 #include "iexp_table.h"
 
-__device__ __forceinline__ double iexp_neg(double x) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-  const int ex = (int)((bits >> 52) & 0x7FF);
-  if (ex < 969) return 1.0;  // |x| < 2^-54 rounds to 1 (also +-0 and subnormals)
-  if (!(x >= -745.1332191019412)) return (x != x) ? x : 0.0;  // underflow, -inf, NaN
-  if (x > 0.0) return exp(x);
-  const unsigned long long M = (bits & 0xFFFFFFFFFFFFFULL) | 0x10000000000000ULL;
+// exp(-|x|) for |x| = M 2^e2 with M normalised (bit 63 set), 2^-54 <= |x| < 1024
+__device__ __forceinline__ double iexp_core(unsigned long long M, int e2) {
   const unsigned __int128 P = (unsigned __int128)M * IEXP_L2E_HI +
                               (unsigned long long)(((unsigned __int128)M * IEXP_L2E_LO) >> 64);
-  const unsigned __int128 Y = P >> (1074 - ex);  // |y| 2^64 (shift 42..105)
+  const unsigned __int128 Y = P >> (-1 - e2);  // |y| 2^64; P = |y| 2^(63 - e2), shift 53..116
   const unsigned int yi = (unsigned int)(Y >> 64);
   const unsigned long long yf = (unsigned long long)Y;
   const unsigned int m = yi + (yf ? 1u : 0u);
@@ -48,4 +44,24 @@ __device__ __forceinline__ double iexp_neg(double x) {
   if (tot > 64) return 0.0;
   const unsigned long long mant = (tot == 64) ? (Z >> 63) : ((Z + (1ULL << (tot - 1))) >> tot);
   return __longlong_as_double((long long)mant);
+}
+
+__device__ __forceinline__ double iexp_neg(double x) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  if (ex < 969) return 1.0;  // |x| < 2^-54 rounds to 1 (also +-0 and subnormals)
+  if (!(x >= -745.1332191019412)) return (x != x) ? x : 0.0;  // underflow, -inf, NaN
+  if (x > 0.0) return exp(x);
+  const unsigned long long M = ((bits & 0xFFFFFFFFFFFFFULL) | 0x10000000000000ULL) << 11;
+  return iexp_core(M, ex - 1086);
+}
+
+// exp(-E 2^e) for an exact non-negative integer E
+__device__ __forceinline__ double iexp_fixed(unsigned long long E, int e) {
+  if (E == 0) return 1.0;
+  const int lz = __clzll((long long)E);
+  const int top = 63 - lz + e;  // 2^top <= E 2^e < 2^(top + 1)
+  if (top >= 10) return 0.0;    // beyond 1024: exp underflows
+  if (top < -55) return 1.0;    // below 2^-55: rounds to 1
+  return iexp_core(E << lz, e - lz);
 }

@@ -26,6 +26,7 @@
 // The diagonal 128 x 128 factor, the panel solve and the right-hand-side
 // (border) rows stay in FP64.
 #include "fgpu_internal.h"
+#include "tc_common.cuh"
 
 #include <cuda.h>
 #include <cuda_fp16.h>
@@ -35,91 +36,6 @@
 #include <mutex>
 
 namespace fgpu {
-
-namespace {
-
-__device__ __forceinline__ uint32_t su32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int it = 0; it < (1 << 22); ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(su32(bar)), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
-}
-
-// one non-blocking probe of an mbarrier phase
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(su32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// tcgen05 shared-memory descriptor, no swizzle, K-major core matrices
-// (8 rows x 16 bytes): lbo = byte stride between core matrices along K,
-// sbo = along M/N; descriptor version 1 (bits 46-47).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
-}
-// kind::f16 instruction descriptor: f32 accumulator, f16 A/B, both K-major, M=128, N=64.
-constexpr uint32_t IDESC_128x64 = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
-
-__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(IDESC_128x64), "r"(accumulate));
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
-               : "memory");
-}
-
-// round(x * 2^(55 - e)) for |x| <= 2^e, with integer operations only.
-// Sets *bad when the scale bound is violated (|x| > 2^(e+3)).
-__device__ __forceinline__ long long to_fixed55(double x, int e, bool* bad) {
-  const long long bits = __double_as_longlong(x);
-  const int E = (int)((bits >> 52) & 0x7FF);
-  if (E == 0) return 0;  // zero or subnormal (below 2^-1022: far under the 2^-55 resolution)
-  if (E == 0x7FF) {
-    *bad = true;
-    return 0;
-  }
-  const long long M = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
-  const int sh = E - 1075 + 55 - e;
-  long long F;
-  if (sh >= 0) {
-    if (sh > 3) {
-      *bad = true;
-      return 0;
-    }
-    F = M << sh;
-  } else if (sh > -63) {
-    F = (M + (1LL << (-sh - 1))) >> (-sh);
-  } else {
-    F = 0;
-  }
-  return bits < 0 ? -F : F;
-}
-
-}  // namespace
 
 // ---------------------------------------------------------------------------
 // per-row scales from the diagonal of K
@@ -314,10 +230,12 @@ __global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, i
 //
 // Output tiles are 128 rows x 64 columns; a tile's 7 level sums occupy 448
 // TMEM columns.  Warp 8 (one lane) streams the digit planes of each k-chunk
-// of 16 by 5-D TMA into a 5-stage ring; warp 9 (one lane) issues the 28
+// of 16 by 5-D TMA into a 3-stage ring and bulk-copies the tile's
+// accumulators (96 KB) into shared memory as soon as the previous tile's
+// epilogue has released that buffer; warp 9 (one lane) issues the 28
 // tcgen05.mma of a chunk; warps 0-7 drain TMEM into registers, release it
-// (so the next tile's MMAs start), then add the tile into the int64/int32
-// accumulators in HBM while the tensor cores work on the next tile.
+// (so the next tile's MMAs start), then add the tile to the accumulators
+// and write them back to HBM while the tensor cores work on the next tile.
 //
 // Accumulator per element: W = hi * 2^24 + lo, hi int64, lo in [0, 2^24),
 // value = W * 2^(e_i + e_j - 62); tile-major storage (128 x 64 tiles,
@@ -326,56 +244,10 @@ __global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, i
 // ---------------------------------------------------------------------------
 constexpr int CH = 8;                                // k-chunks of 16 per 128-panel (one MMA each)
 constexpr int NSTAGE = 3;
-constexpr uint32_t A_STAGE = NSLICE * 4096;          // 7 planes x 2 k-groups x 128 rows x 16 B
-constexpr uint32_t B_STAGE = NSLICE * 2048;          // 7 planes x 2 k-groups x 64 rows x 16 B
-constexpr uint32_t STAGE = A_STAGE + B_STAGE;        // 43008 B
 constexpr uint32_t ACC_HI_TILE = 128 * 64 * 8;       // accumulator tile, high words (64 KB)
 constexpr uint32_t ACC_LO_TILE = 128 * 64 * 4;       // low 24-bit words (32 KB)
 constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + ACC_HI_TILE + ACC_LO_TILE + 256;
 constexpr int UPD_THREADS = 320;
-
-__device__ __forceinline__ void tma_load_5d(void* dst, const void* tmap, int c0, int c1, int c2, int c3, int c4,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
-      "%6}], [%7];" ::"r"(su32(dst)),
-      "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(su32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(su32(dst)),
-      "l"(src), "r"(bytes), "r"(su32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
-}
-
-// tile t of step s -> (problem, 128-row tile, 64-column tile); false if out of range
-__device__ __forceinline__ bool decode_tile(const Prob* __restrict__ probs, const int* __restrict__ prefix, int nprob,
-                                            int s, int t, int& p, int& ti, int& tj) {
-  if (t >= prefix[nprob]) return false;
-  int lo = 0, hi = nprob;  // largest p with prefix[p] <= t
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (prefix[mid] <= t) lo = mid; else hi = mid;
-  }
-  p = lo;
-  const int m = probs[p].nt128 - s - 1;
-  int r = t - prefix[p];
-  // column-tile pair q (tj = 2(s+1)+2q, +1) holds 2 (m - q) tiles
-  int q = 0;
-  while (r >= 2 * (m - q)) {
-    r -= 2 * (m - q);
-    ++q;
-  }
-  const int half = r >= (m - q) ? 1 : 0;
-  const int rr = r - half * (m - q);
-  tj = 2 * (s + 1) + 2 * q + half;
-  ti = s + 1 + q + rr;
-  return true;
-}
 
 __global__ void __launch_bounds__(UPD_THREADS, 1)
     k_ozaki_update(const Prob* __restrict__ probs, int nprob, int s, const int* __restrict__ prefix) {

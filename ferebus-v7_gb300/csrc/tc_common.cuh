@@ -1,0 +1,144 @@
+// Shared device helpers of the tcgen05 kernels: mbarriers with bounded waits,
+// shared-memory matrix descriptors, kind::f16 MMA issue and commit, TMA and
+// bulk copies, the FP64 -> 55-bit fixed-point conversion, and the tile
+// enumeration of a lower-triangular block range.
+#pragma once
+#include "fgpu_internal.h"
+
+#include <cuda_fp16.h>
+
+namespace fgpu {
+namespace {
+
+// one k-chunk of 16 of the digit planes in shared memory (no swizzle,
+// K-major core matrices): A = 128 rows, B = 64 rows, 7 planes each
+constexpr uint32_t A_STAGE = NSLICE * 4096;  // 7 planes x 2 k-groups x 128 rows x 16 B
+constexpr uint32_t B_STAGE = NSLICE * 2048;  // 7 planes x 2 k-groups x 64 rows x 16 B
+constexpr uint32_t STAGE = A_STAGE + B_STAGE;  // 43008 B
+
+__device__ __forceinline__ uint32_t su32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(su32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// one non-blocking probe of an mbarrier phase
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(su32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// tcgen05 shared-memory descriptor, no swizzle, K-major core matrices
+// (8 rows x 16 bytes): lbo = byte stride between core matrices along K,
+// sbo = along M/N; descriptor version 1 (bits 46-47).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+// kind::f16 instruction descriptor: f32 accumulator, f16 A/B, both K-major, M=128, N=64.
+constexpr uint32_t IDESC_128x64 = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC_128x64), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
+               : "memory");
+}
+
+// round(x * 2^(55 - e)) for |x| <= 2^e, with integer operations only.
+// Sets *bad when the scale bound is violated (|x| > 2^(e+3)).
+__device__ __forceinline__ long long to_fixed55(double x, int e, bool* bad) {
+  const long long bits = __double_as_longlong(x);
+  const int E = (int)((bits >> 52) & 0x7FF);
+  if (E == 0) return 0;  // zero or subnormal (below 2^-1022: far under the 2^-55 resolution)
+  if (E == 0x7FF) {
+    *bad = true;
+    return 0;
+  }
+  const long long M = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+  const int sh = E - 1075 + 55 - e;
+  long long F;
+  if (sh >= 0) {
+    if (sh > 3) {
+      *bad = true;
+      return 0;
+    }
+    F = M << sh;
+  } else if (sh > -63) {
+    F = (M + (1LL << (-sh - 1))) >> (-sh);
+  } else {
+    F = 0;
+  }
+  return bits < 0 ? -F : F;
+}
+
+__device__ __forceinline__ void tma_load_5d(void* dst, const void* tmap, int c0, int c1, int c2, int c3, int c4,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+      "%6}], [%7];" ::"r"(su32(dst)),
+      "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(su32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(su32(dst)),
+      "l"(src), "r"(bytes), "r"(su32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+
+// tile t of step s -> (problem, 128-row tile, 64-column tile); false if out of range
+__device__ __forceinline__ bool decode_tile(const Prob* __restrict__ probs, const int* __restrict__ prefix, int nprob,
+                                            int s, int t, int& p, int& ti, int& tj) {
+  if (t >= prefix[nprob]) return false;
+  int lo = 0, hi = nprob;  // largest p with prefix[p] <= t
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  p = lo;
+  const int m = probs[p].nt128 - s - 1;
+  int r = t - prefix[p];
+  // column-tile pair q (tj = 2(s+1)+2q, +1) holds 2 (m - q) tiles
+  int q = 0;
+  while (r >= 2 * (m - q)) {
+    r -= 2 * (m - q);
+    ++q;
+  }
+  const int half = r >= (m - q) ? 1 : 0;
+  const int rr = r - half * (m - q);
+  tj = 2 * (s + 1) + 2 * q + half;
+  ti = s + 1 + q + rr;
+  return true;
+}
+
+}  // namespace
+}  // namespace fgpu

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libfgpu.so")
 
-SOURCES = ["engine.cu", "api.cu", "noalloc.cu", "ozaki.cu", "grad.cu"]
+SOURCES = ["engine.cu", "api.cu", "noalloc.cu", "ozaki.cu", "grad.cu", "build_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-fmad=true", 
               "-Xptxas", "-O3"]
