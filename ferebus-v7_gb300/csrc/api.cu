@@ -145,6 +145,8 @@ struct UpdSched {
   int num_sms = 0;
   int* build_prefix_dev = nullptr;  // nprob + 1: tiles of the tensor-core build
   int build_total = 0;
+  int* row_prefix_dev = nullptr;    // per step, nprob + 1: 128-row tiles ti >= step (quarter coupling)
+  std::vector<int> row_totals;
 };
 
 struct Workspace {
@@ -159,7 +161,7 @@ struct Workspace {
   long long* acc_hi = nullptr;
   int* acc_lo = nullptr;
   unsigned char* slices = nullptr;
-  unsigned char* tmaps = nullptr;  // 2 x 128 B TMA tensor maps over slices
+  unsigned char* tmaps = nullptr;  // 3 x 128 B TMA tensor maps over slices (128-, 64-, 32-row boxes)
   double* splanes = nullptr;       // theta-scaled planes (dot-product build)
   double* norms = nullptr;
   long long* fnorm = nullptr;      // tensor-core build: W_ii of the distance leaves
@@ -295,6 +297,7 @@ void fill_prob(Prob& p, const fgpu_ctx* c, const double* theta_d, const Workspac
   p.slices = ws.slices;
   p.tmap_a = ws.tmaps;
   p.tmap_b = ws.tmaps ? ws.tmaps + 128 : nullptr;
+  p.tmap_b32 = ws.tmaps ? ws.tmaps + 256 : nullptr;
   p.splanes = ws.splanes;
   p.norms = ws.norms;
   p.plane_max = c->plane_max_d;
@@ -327,6 +330,23 @@ int build_sched(const std::vector<int>& nt128, const std::vector<int>& tc_build,
   CK(cudaMalloc(&u.prefix_dev, sizeof(int) * h.size()));
   if (track) track->push_back(u.prefix_dev);
   CK(cudaMemcpy(u.prefix_dev, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
+  // quarter coupling: row tiles ti >= step of every problem
+  {
+    std::vector<int> r((size_t)std::max(ntmax, 1) * u.stride, 0);
+    u.row_totals.assign(std::max(ntmax, 1), 0);
+    for (int st = 0; st < ntmax; ++st) {
+      int acc = 0;
+      for (int p = 0; p < nprob; ++p) {
+        r[(size_t)st * u.stride + p] = acc;
+        acc += std::max(0, nt128[p] - st);
+      }
+      r[(size_t)st * u.stride + nprob] = acc;
+      u.row_totals[st] = acc;
+    }
+    CK(cudaMalloc(&u.row_prefix_dev, sizeof(int) * r.size()));
+    if (track) track->push_back(u.row_prefix_dev);
+    CK(cudaMemcpy(u.row_prefix_dev, r.data(), sizeof(int) * r.size(), cudaMemcpyHostToDevice));
+  }
   // tensor-core build: the whole lower triangle, nt128 (nt128 + 1) tiles of 128 x 64
   std::vector<int> b(nprob + 1, 0);
   for (int p = 0; p < nprob; ++p) b[p + 1] = b[p] + (tc_build[p] ? nt128[p] * (nt128[p] + 1) : 0);
@@ -375,20 +395,23 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
     if (us->build_total > 0)
       STAGE(0, launch_build_tc(probs_d, nprob, us->build_prefix_dev, us->build_total, us->num_sms, s));
     STAGE(0, launch_scales(probs_d, nprob, max_nc, s));
+    const int max_rows = max_nc + TB;  // the tallest problem's ld: factor rows + right-hand sides
     for (int step = 0; step < nt; ++step) {
       if (step > 0) STAGE(5, launch_panel_prep(probs_d, nprob, step, max_nc, s));
-      // first 64-column half: FP64 diagonal factor + panel solve
-      STAGE(1, launch_potf2(probs_d, nprob, 2 * step, s));
-      STAGE(2, launch_trsm(probs_d, nprob, 2 * step, max_nsteps, s));
-      // coupling into the second half on the tensor cores
-      STAGE(6, launch_split_half(probs_d, nprob, step, nt, s));
-      STAGE(6, launch_gemm_half(probs_d, nprob, step, nt, s));
-      STAGE(7, launch_border_half(probs_d, nprob, step, s));
-      // second half
-      STAGE(1, launch_potf2(probs_d, nprob, 2 * step + 1, s));
-      STAGE(2, launch_trsm(probs_d, nprob, 2 * step + 1, max_nsteps, s));
+      // four 32-column quarters: FP64 diagonal factor, panel solve and digit
+      // planes of each; tensor-core couplings quarter 0 -> 1, half 0 -> 1,
+      // quarter 2 -> 3 before the quarter that needs them
+      const int* rows_prefix = us->row_prefix_dev + (size_t)step * us->stride;
+      const int rows_total = us->row_totals[step];
+      for (int q = 0; q < NB / QW; ++q) {
+        if (q == 1) STAGE(8, launch_couple(probs_d, nprob, step, 0, 1, 1, 1, rows_prefix, rows_total, us->num_sms, s));
+        if (q == 2) STAGE(8, launch_couple(probs_d, nprob, step, 0, 2, 2, 2, rows_prefix, rows_total, us->num_sms, s));
+        if (q == 3) STAGE(8, launch_couple(probs_d, nprob, step, 2, 1, 3, 1, rows_prefix, rows_total, us->num_sms, s));
+        STAGE(1, launch_potf2_quarter(probs_d, nprob, step, q, s));
+        STAGE(2, launch_trsm_quarter(probs_d, nprob, step, q, max_rows, s));
+        STAGE(6, launch_split_quarter(probs_d, nprob, step, q, nt, s));
+      }
       if (step + 1 < nt) {
-        STAGE(6, launch_split(probs_d, nprob, step, nt, s));
         STAGE(3, launch_ozaki_update(probs_d, nprob, step, nt, us->prefix_dev + (size_t)step * us->stride,
                                      us->totals[step], us->num_sms, s));
         STAGE(7, launch_border_update(probs_d, nprob, step, max_nc, s));
@@ -431,7 +454,8 @@ int capture(cudaStream_t s, cudaGraphExec_t* exec, const Prob* probs_d, int npro
 
 int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track) {
   CK(cudaMalloc(&ws.K, K_elems(c) * sizeof(double)));
-  CK(cudaMalloc(&ws.logdet_part, sizeof(double) * (c->nsteps + 1)));
+  // one log-det part per 64-column block (FP64 mode) or 32-column quarter (tensor-core mode)
+  CK(cudaMalloc(&ws.logdet_part, sizeof(double) * 2 * (c->nsteps + 1)));
   CK(cudaMalloc(&ws.out, sizeof(double) * 8));
   CK(cudaMalloc(&ws.z, sizeof(double) * c->Nc));
   if (c->mode == 1) {
@@ -447,11 +471,11 @@ int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track)
     CK(cudaMalloc(&ws.fnorm, sizeof(long long) * 2 * nc));
     CK(cudaMalloc(&ws.fcoef, sizeof(double) * 4));
     CK(cudaMalloc(&ws.fscale, sizeof(int) * 2));
-    CK(cudaMalloc(&ws.tmaps, 256));
-    alignas(64) unsigned char maps[256];
+    CK(cudaMalloc(&ws.tmaps, 384));
+    alignas(64) unsigned char maps[384];
     const int er = encode_slice_maps(maps, ws.slices, c->nt128);
     if (er != 0) return fail(FGPU_ECUDA, "cuTensorMapEncodeTiled failed (%d)", er);
-    CK(cudaMemcpy(ws.tmaps, maps, 256, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ws.tmaps, maps, 384, cudaMemcpyHostToDevice));
   }
   if (track) {
     for (void* q : {(void*)ws.K, (void*)ws.logdet_part, (void*)ws.out, (void*)ws.z, (void*)ws.escale,
@@ -485,6 +509,7 @@ void free_worker(Worker* w) {
   cudaFree(w->prob_d);
   cudaFree(w->sched.prefix_dev);
   cudaFree(w->sched.build_prefix_dev);
+  cudaFree(w->sched.row_prefix_dev);
   if (w->h_stage) cudaFreeHost(w->h_stage);
   if (w->stream) cudaStreamDestroy(w->stream);
   delete w;

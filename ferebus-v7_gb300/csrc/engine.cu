@@ -418,33 +418,38 @@ __global__ void __launch_bounds__(256) k_build_dot(const Prob* __restrict__ prob
 // ---------------------------------------------------------------------------
 // diagonal block factorisation (blocked, left-looking) + log-det partial
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_potf2(const Prob* __restrict__ probs, int step) {
-  // Blocked left-looking factorisation of the 64 x 64 diagonal block in
-  // shared memory, panels of 8 columns (the dot-product order of LAPACK's
-  // dpotf2, lapack/dpotf2.f): (a) the panel minus the finished columns times
-  // their rows, all threads; (b) the 8 x 8 diagonal block by one warp in
-  // registers (shuffles, no block barriers); (c) the rows below by forward
-  // substitution, one thread per row.  Three block barriers per panel.
+// W x W block at (col0, col0); W * 4 threads; writes the block's sum of
+// log(L_cc) to logdet_part[part].
+template <int W>
+__global__ void __launch_bounds__(W * 4) k_potf2w(const Prob* __restrict__ probs, int col0_step, int col0_off,
+                                                  int part_step, int part_off) {
+  // Blocked left-looking factorisation in shared memory, panels of 8
+  // columns (the dot-product order of LAPACK's dpotf2, lapack/dpotf2.f):
+  // (a) the panel minus the finished columns times their rows, all threads;
+  // (b) the 8 x 8 diagonal block by one warp in registers (shuffles, no
+  // block barriers); (c) the rows below by forward substitution, one thread
+  // per row.  Three block barriers per panel.
   const Prob& P = probs[blockIdx.x];
-  if (step >= P.nsteps) return;
+  const int col0 = col0_step + col0_off;
+  if (col0 >= P.Nc) return;
   if (*(volatile int*)&P.status[1]) return;
-  constexpr int LDA = TB + 1;
-  __shared__ double A[TB * LDA];  // A[c * LDA + r]
-  __shared__ double rdg[TB];      // 1 / L_cc
+  constexpr int LDA = W + 1;
+  __shared__ double A[W * LDA];  // A[c * LDA + r]
+  __shared__ double rdg[W];      // 1 / L_cc
   __shared__ int fail_col;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const size_t ld = (size_t)P.ld;
-  double* Kd = P.K + (size_t)(step * TB) * ld + step * TB;
-  for (int e = tid; e < TB * TB; e += blockDim.x) {
-    const int r = e % TB, c = e / TB;
+  double* Kd = P.K + (size_t)col0 * ld + col0;
+  for (int e = tid; e < W * W; e += blockDim.x) {
+    const int r = e % W, c = e / W;
     A[c * LDA + r] = Kd[(size_t)c * ld + r];
   }
   if (tid == 0) fail_col = -1;
   __syncthreads();
-  for (int c0 = 0; c0 < TB; c0 += 8) {
+  for (int c0 = 0; c0 < W; c0 += 8) {
     // (a) columns c0..c0+7, rows >= column: subtract sum_{k < c0} L_rk L_ck
     if (c0 > 0) {
-      const int r = tid & (TB - 1), cp = c0 + 2 * (tid >> 6);
+      const int r = tid % W, cp = c0 + 2 * (tid / W);
       if (r >= cp) {
         double a0 = A[cp * LDA + r], a1 = A[(cp + 1) * LDA + r];
         for (int k = 0; k < c0; ++k) {
@@ -489,7 +494,7 @@ __global__ void __launch_bounds__(256) k_potf2(const Prob* __restrict__ probs, i
     __syncthreads();
     if (fail_col >= 0) break;
     // (c) rows below the diagonal block: forward substitution over the panel
-    if (tid < TB - c0 - 8) {
+    if (tid < W - c0 - 8) {
       const int r = c0 + 8 + tid;
       double x[8];
 #pragma unroll
@@ -505,62 +510,72 @@ __global__ void __launch_bounds__(256) k_potf2(const Prob* __restrict__ probs, i
   }
   if (fail_col >= 0) {
     if (tid == 0) {
-      P.status[0] = step * TB + fail_col + 1;  // LAPACK info: 1-based column
+      P.status[0] = col0 + fail_col + 1;  // LAPACK info: 1-based column
       P.status[1] = 1;
     }
     return;
   }
-  for (int e = tid; e < TB * TB; e += blockDim.x) {
-    const int r = e % TB, c = e / TB;
+  for (int e = tid; e < W * W; e += blockDim.x) {
+    const int r = e % W, c = e / W;
     if (r >= c) Kd[(size_t)c * ld + r] = A[c * LDA + r];
   }
   // log-det partial: 2 * sum log(L_jj) is formed in the epilogue
   // (arith.f90:72-93); here the block's sum of logs, in column order.
   if (tid < 32) {
-    double sl = log(A[(2 * tid) * LDA + 2 * tid]) + log(A[(2 * tid + 1) * LDA + 2 * tid + 1]);
+    double sl = 0.0;
+    for (int c = tid * (W / 32); c < (tid + 1) * (W / 32); ++c) sl += log(A[c * LDA + c]);
     for (int o = 16; o > 0; o >>= 1) sl += __shfl_down_sync(0xffffffffu, sl, o);
-    if (tid == 0) P.logdet_part[step] = sl;
+    if (tid == 0) P.logdet_part[part_step + part_off] = sl;
   }
 }
 
 // ---------------------------------------------------------------------------
-// panel solve: A21 <- A21 * L11^-T for the row tiles below the diagonal block
-// (including the border tile of right-hand sides)
+// panel solve: A21 <- A21 * L11^-T for the rows below the W x W diagonal
+// block at col0, in tiles of 64 rows (including the border rows of
+// right-hand sides; rows past the last 64-row tile of the problem are skipped)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_trsm(const Prob* __restrict__ probs, int step) {
+template <int W>
+__global__ void __launch_bounds__(256) k_trsmw(const Prob* __restrict__ probs, int col0_step, int col0_off) {
   const Prob& P = probs[blockIdx.y];
-  const int ti = step + 1 + blockIdx.x;
+  const int col0 = col0_step + col0_off;
   const int last = P.nrt ? P.nrt - 1 : P.nsteps;  // last 64-row tile
-  if (step >= P.nsteps || ti > last) return;
+  const int row_end = (last + 1) * TB;
+  const int r0 = col0 + W + blockIdx.x * TB;
+  if (col0 >= P.Nc || r0 >= row_end) return;
   if (*(volatile int*)&P.status[1]) return;
-  __shared__ double L[TB * (TB + 1)];
-  __shared__ double B[TB * (TB + 1)];
-  __shared__ double rd[TB];
+  constexpr int LDA = TB + 1;
+  __shared__ double L[W * (W + 1)];
+  __shared__ double B[W * LDA];
+  __shared__ double rd[W];
   const int tid = threadIdx.x;
   const size_t ld = (size_t)P.ld;
-  const double* Ld = P.K + (size_t)(step * TB) * ld + step * TB;
-  double* Bd = P.K + (size_t)(step * TB) * ld + ti * TB;
-  for (int e = tid; e < TB * TB; e += blockDim.x) {
+  const int nr = min(TB, row_end - r0);
+  const double* Ld = P.K + (size_t)col0 * ld + col0;
+  double* Bd = P.K + (size_t)col0 * ld + r0;
+  for (int e = tid; e < W * W; e += blockDim.x) {
+    const int r = e % W, c = e / W;
+    L[c * (W + 1) + r] = Ld[(size_t)c * ld + r];
+  }
+  for (int e = tid; e < TB * W; e += blockDim.x) {
     const int r = e % TB, c = e / TB;
-    L[c * (TB + 1) + r] = Ld[(size_t)c * ld + r];
-    B[c * (TB + 1) + r] = Bd[(size_t)c * ld + r];
+    B[c * LDA + r] = r < nr ? Bd[(size_t)c * ld + r] : 0.0;
   }
   __syncthreads();
-  if (tid < TB) rd[tid] = 1.0 / L[tid * (TB + 1) + tid];
+  if (tid < W) rd[tid] = 1.0 / L[tid * (W + 1) + tid];
   __syncthreads();
-  for (int c = 0; c < TB; ++c) {
-    if (tid < TB) B[c * (TB + 1) + tid] *= rd[c];
+  for (int c = 0; c < W; ++c) {
+    if (tid < TB) B[c * LDA + tid] *= rd[c];
     __syncthreads();
-    const int w = TB - 1 - c;
+    const int w = W - 1 - c;
     for (int e = tid; e < w * TB; e += blockDim.x) {
       const int r = e % TB, q = c + 1 + e / TB;
-      B[q * (TB + 1) + r] = fma(-B[c * (TB + 1) + r], L[c * (TB + 1) + q], B[q * (TB + 1) + r]);
+      B[q * LDA + r] = fma(-B[c * LDA + r], L[c * (W + 1) + q], B[q * LDA + r]);
     }
     __syncthreads();
   }
-  for (int e = tid; e < TB * TB; e += blockDim.x) {
+  for (int e = tid; e < TB * W; e += blockDim.x) {
     const int r = e % TB, c = e / TB;
-    Bd[(size_t)c * ld + r] = B[c * (TB + 1) + r];
+    if (r < nr) Bd[(size_t)c * ld + r] = B[c * LDA + r];
   }
 }
 
@@ -671,7 +686,8 @@ __global__ void __launch_bounds__(256) k_finalize(const Prob* __restrict__ probs
   const double* z1 = P.K + P.Nc + 1;  // row Nc+1: ones (concentrated)
   double logdet = 0.0;
   if (tid == 0) {
-    for (int s = 0; s < P.nsteps; ++s) logdet += P.logdet_part[s];
+    const int nparts = P.mode == 1 ? P.Nc / QW : P.nsteps;  // 32-column parts in tensor-core mode
+    for (int s = 0; s < nparts; ++s) logdet += P.logdet_part[s];
     logdet *= 2.0;
   }
   double ll, mean = 0.0, s2 = 0.0;
@@ -792,7 +808,20 @@ cudaError_t launch_build_dot(const Prob* probs, int nprob, int max_nsteps, int m
 }
 
 cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s) {
-  k_potf2<<<nprob, 256, 0, s>>>(probs, step);
+  k_potf2w<TB><<<nprob, TB * 4, 0, s>>>(probs, step * TB, 0, step, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_potf2_quarter(const Prob* probs, int nprob, int step, int q, cudaStream_t s) {
+  // log-det parts indexed by 32-column block
+  k_potf2w<QW><<<nprob, QW * 4, 0, s>>>(probs, step * NB, q * QW, step * (NB / QW), q);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trsm_quarter(const Prob* probs, int nprob, int step, int q, int max_rows, cudaStream_t s) {
+  const int rows = max_rows - (step * NB + q * QW + QW);
+  if (rows <= 0) return cudaSuccess;
+  k_trsmw<QW><<<dim3((rows + TB - 1) / TB, nprob), 256, 0, s>>>(probs, step * NB, q * QW);
   return cudaGetLastError();
 }
 
@@ -801,7 +830,7 @@ cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, 
   if (max_rowtiles <= 0) max_rowtiles = max_nsteps + 1;
   const int rows = max_rowtiles - step - 1;  // row tiles step+1 .. last (incl. border rows)
   if (rows <= 0) return cudaSuccess;
-  k_trsm<<<dim3(rows, nprob), 256, 0, s>>>(probs, step);
+  k_trsmw<TB><<<dim3(rows, nprob), 256, 0, s>>>(probs, step * TB, 0);
   return cudaGetLastError();
 }
 

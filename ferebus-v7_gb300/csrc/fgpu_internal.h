@@ -81,6 +81,7 @@ struct Prob {
   unsigned char* slices;          // nt128 x 7 x 32 KB: fp16 digit planes of the current panel
   const void* tmap_a;             // TMA tensor map over slices, box 8 x 128 rows x 2 kgroups x 7 planes
   const void* tmap_b;             // same, box of 64 rows
+  const void* tmap_b32;           // same, box of 32 rows (quarter-panel coupling)
   // dot-product kernel build (mode 1): planes scaled by sqrt(l_k) per evaluation
   double* splanes;                // nplanes x Nc
   double* norms;                  // MAX_LEAF x Nc: sum_k u_ik^2 of rbf leaves
@@ -96,8 +97,9 @@ struct Prob {
   int* fscale;                    // 2: s of the distance leaves, max |f| < 2^s
 };
 
-// Encode the two 5-D TMA tensor maps of a problem's digit-plane buffer into
-// host memory (2 x 128 bytes).  Returns 0 or a CUDA driver error code.
+// Encode the three 5-D TMA tensor maps of a problem's digit-plane buffer
+// (boxes of 128, 64 and 32 rows) into host memory (3 x 128 bytes).  Returns 0
+// or a CUDA driver error code.
 int encode_slice_maps(void* host_maps, const void* slices, int nt128);
 
 // Launch helpers (engine.cu).  All kernels take a device array of problems
@@ -109,6 +111,11 @@ cudaError_t launch_prep_planes(const Prob* probs, int nprob, int max_nc, cudaStr
 cudaError_t launch_build_dot(const Prob* probs, int nprob, int max_nsteps, int max_nplanes, cudaStream_t s);
 size_t build_dot_smem_bytes(int nplanes);
 cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s);
+// tensor-core mode: the 32 x 32 diagonal block of quarter q of panel step, and
+// the rows below it up to max_rows (the tallest problem's ld)
+constexpr int QW = 32;
+cudaError_t launch_potf2_quarter(const Prob* probs, int nprob, int step, int q, cudaStream_t s);
+cudaError_t launch_trsm_quarter(const Prob* probs, int nprob, int step, int q, int max_rows, cudaStream_t s);
 // max_rowtiles: 64-row tiles of the tallest problem (0 = max_nsteps + 1)
 cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s,
                         int max_rowtiles = 0);
@@ -125,20 +132,19 @@ constexpr int NSLICE = 7;                       // fp16 digit planes per FP64 va
 constexpr size_t SLICE_BYTES = 128 * 128 * 2;   // one digit plane of a 128-row x 128-k tile
 cudaError_t launch_scales(const Prob* probs, int nprob, int max_nc, cudaStream_t s);
 cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
-cudaError_t launch_potf2_128(const Prob* probs, int nprob, int step, cudaStream_t s);
-cudaError_t launch_trsm128(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
-cudaError_t launch_split(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
 // prefix: device table of nprob + 1 tile offsets for this step (tiles of
 // problem p at step s: m (m + 1), m = nt128_p - s - 1); total_tiles = prefix[nprob].
 cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, const int* prefix,
                                 int total_tiles, int num_sms, cudaStream_t s);
 cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
-// two 64-column halves per 128-panel: digit planes of the first half (rows
-// from the panel's own row tile), their tensor-core coupling into the second
-// half, and the FP64 coupling of the right-hand-side rows
-cudaError_t launch_split_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
-cudaError_t launch_gemm_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s);
-cudaError_t launch_border_half(const Prob* probs, int nprob, int step, cudaStream_t s);
+// four 32-column quarters per 128-panel: digit planes of quarter q (rows from
+// the panel's own row tile), and the tensor-core coupling of source quarters
+// [sq, sq + ns) into destination quarters [dq, dq + nq), nq = 1 or 2 (with
+// the right-hand-side rows in FP64).  prefix: nprob + 1 offsets of the row
+// tiles ti >= step of each problem.
+cudaError_t launch_split_quarter(const Prob* probs, int nprob, int step, int q, int max_nt128, cudaStream_t s);
+cudaError_t launch_couple(const Prob* probs, int nprob, int step, int sq, int ns, int dq, int nq,
+                          const int* prefix, int total_tiles, int num_sms, cudaStream_t s);
 
 // Tensor-core kernel-matrix build (build_tc.cu): feature digit planes and
 // exact self products, then the persistent build of the lower triangle.

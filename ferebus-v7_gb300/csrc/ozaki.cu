@@ -65,139 +65,26 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
   const int i = c0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.Nc) return;
   const size_t ld = (size_t)P.ld;
-  const double pi = P.pw2[i];
+  const int ei = P.escale[i] - 62;
   for (int jj = 0; jj < 16; ++jj) {
     const int j = c0 + blockIdx.y * 16 + jj;
     const size_t a = ((size_t)((j >> 6) * P.nt128 + (i >> 7)) * 64 + (j & 63)) * 128 + (i & 127);
-    const double w = fma((double)P.acc_hi[a], 16777216.0, (double)P.acc_lo[a]);
+    const double w = fixed_to_double(P.acc_hi[a], P.acc_lo[a], ei + P.escale[j]);
     double* kp = P.K + (size_t)j * ld + i;
-    *kp = *kp - w * pi * P.pw2[j];
+    *kp = *kp - w;
   }
 }
 
 // ---------------------------------------------------------------------------
-// 128 x 128 diagonal block factorisation (FP64) + log-det partial
+// digit planes of panel s, k-groups kg0.. (8 columns each), for the rows of
+// 128-row tiles ti0..; layout per 128-row tile and digit p:
+// [kgroup 16][row 128][8 k] fp16
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) k_potf2_128(const Prob* __restrict__ probs, int s) {
-  const Prob& P = probs[blockIdx.x];
-  if (P.mode != 1 || s >= P.nt128 || P.status[1]) return;
-  extern __shared__ __align__(16) double A[];  // 128 x 129
-  __shared__ double rdiag;
-  __shared__ int fail_col;
-  __shared__ double red[16];
-  constexpr int S = NB + 1;
-  const int tid = threadIdx.x;
-  const size_t ld = (size_t)P.ld;
-  double* Kd = P.K + (size_t)(s * NB) * ld + s * NB;
-  for (int e = tid; e < NB * NB; e += blockDim.x) {
-    const int r = e % NB, c = e / NB;
-    A[c * S + r] = Kd[(size_t)c * ld + r];
-  }
-  if (tid == 0) fail_col = -1;
-  __syncthreads();
-  for (int j = 0; j < NB; ++j) {
-    if (tid == 0) {
-      const double d = A[j * S + j];
-      if (!(d > 0.0)) {
-        fail_col = j;
-      } else {
-        const double sq = sqrt(d);
-        A[j * S + j] = sq;
-        rdiag = 1.0 / sq;
-      }
-    }
-    __syncthreads();
-    if (fail_col >= 0) break;
-    if (tid > j && tid < NB) A[j * S + tid] *= rdiag;
-    __syncthreads();
-    // rank-1 update of the trailing lower triangle: thread (row r, group g)
-    // updates columns c = j+1+g, j+1+g+4, ... <= r
-    {
-      const int r = tid & (NB - 1), g = tid >> 7;
-      if (r > j) {
-        const double ljr = A[j * S + r];
-        for (int c = j + 1 + g; c <= r; c += 4) A[c * S + r] = fma(-ljr, A[j * S + c], A[c * S + r]);
-      }
-    }
-    __syncthreads();
-  }
-  if (fail_col >= 0) {
-    if (tid == 0) {
-      P.status[0] = s * NB + fail_col + 1;
-      P.status[1] = 1;
-    }
-    return;
-  }
-  for (int e = tid; e < NB * NB; e += blockDim.x) {
-    const int r = e % NB, c = e / NB;
-    if (r >= c) Kd[(size_t)c * ld + r] = A[c * S + r];
-  }
-  // log-det partial in the slots of the two 64-column halves
-  double v = tid < NB ? log(A[tid * S + tid]) : 0.0;
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((tid & 31) == 0) red[tid >> 5] = v;
-  __syncthreads();
-  if (tid == 0) {
-    double t = 0.0;
-    for (int w = 0; w < 4; ++w) t += red[w];
-    P.logdet_part[2 * s] = t;
-    P.logdet_part[2 * s + 1] = 0.0;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// panel solve with the 128-wide L11 (FP64), 64-row tiles incl. the border tile
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_trsm128(const Prob* __restrict__ probs, int s) {
-  const Prob& P = probs[blockIdx.y];
-  const int ti = 2 * (s + 1) + blockIdx.x;  // 64-row tile index; P.nsteps is the border tile
-  if (P.mode != 1 || s >= P.nt128 || ti > P.nsteps || P.status[1]) return;
-  extern __shared__ __align__(16) double smd[];
-  constexpr int S = NB + 1;   // L11: 128 x 128, column stride 129
-  constexpr int SB = TB + 1;  // panel rows: 64 x 128, column stride 65
-  double* L = smd;
-  double* B = smd + NB * S;
-  double* rd = B + NB * SB;
-  const int tid = threadIdx.x;
-  const size_t ld = (size_t)P.ld;
-  const double* Ld = P.K + (size_t)(s * NB) * ld + s * NB;
-  double* Bd = P.K + (size_t)(s * NB) * ld + ti * TB;
-  for (int e = tid; e < NB * NB; e += blockDim.x) {
-    const int r = e % NB, c = e / NB;
-    L[c * S + r] = Ld[(size_t)c * ld + r];
-  }
-  for (int e = tid; e < TB * NB; e += blockDim.x) {
-    const int r = e % TB, c = e / TB;
-    B[c * SB + r] = Bd[(size_t)c * ld + r];
-  }
-  __syncthreads();
-  if (tid < NB) rd[tid] = 1.0 / L[tid * S + tid];
-  __syncthreads();
-  for (int c = 0; c < NB; ++c) {
-    if (tid < TB) B[c * SB + tid] *= rd[c];
-    __syncthreads();
-    const int w = NB - 1 - c;
-    for (int e = tid; e < w * TB; e += blockDim.x) {
-      const int r = e % TB, q = c + 1 + e / TB;
-      B[q * SB + r] = fma(-B[c * SB + r], L[c * S + q], B[q * SB + r]);
-    }
-    __syncthreads();
-  }
-  for (int e = tid; e < TB * NB; e += blockDim.x) {
-    const int r = e % TB, c = e / TB;
-    Bd[(size_t)c * ld + r] = B[c * SB + r];
-  }
-}
-
-// ---------------------------------------------------------------------------
-// digit planes of the panel rows below the diagonal block
-// layout per 128-row tile and digit p: [kgroup 16][row 128][8 k] fp16
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, int s, int ti0) {
+__global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, int s, int ti0, int kg0) {
   const Prob& P = probs[blockIdx.z];
   const int ti = ti0 + blockIdx.x;
   if (P.mode != 1 || ti >= P.nt128 || P.status[1]) return;
-  const int r = threadIdx.x, kg = blockIdx.y;
+  const int r = threadIdx.x, kg = kg0 + blockIdx.y;
   const int i = ti * NB + r;
   const int e = P.escale[i];
   const size_t ld = (size_t)P.ld;
@@ -455,32 +342,54 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
-// coupling of the two 64-column halves of panel s on the tensor cores:
-// K[i, c0+64+j] -= sum_{k<64} L[i, c0+k] L[c0+64+j, c0+k] for rows i >= c0+64,
-// from the digit planes of the first half (k-groups 0..7).  One CTA per
-// 128-row tile; the exact level sums are converted to FP64 once.
+// coupling inside panel s on the tensor cores: for source quarters
+// [sq, sq + ns) and destination quarters [dq, dq + NQ) (32 columns each),
+//   K[i, c0+32dq+j] -= sum_{k in source} L[i, c0+k] L[c0+32dq+j, c0+k],
+// for rows i >= c0 + 32 dq, from the digit planes of the source quarters.
+// The panel uses three: quarter 0 -> 1, half 0 -> half 1, quarter 2 -> 3.
+// Persistent and warp-specialised like the trailing update: one lane of
+// warp 4 streams the k-chunks of each 128-row tile (A: 128 rows; B: the
+// destination's 32 NQ rows) through a 3-stage ring, one lane of warp 5
+// issues the MMAs (N = 32 NQ) into TMEM (two buffers of 7 x 32 columns for
+// NQ = 1, one of 7 x 64 for NQ = 2), warps 0-3 drain the level sums in groups
+// of 8 columns and subtract the exactly converted sums from K; warp 6 applies
+// the same coupling to the right-hand-side rows in FP64.
 // ---------------------------------------------------------------------------
-constexpr uint32_t HALF_SMEM = 4 * STAGE + 128;
+constexpr int CPL_NSTAGE = 3;
+constexpr uint32_t CPL_SMEM = CPL_NSTAGE * STAGE + 256;
+constexpr int CPL_THREADS = 224;  // warps 0-3 epilogue, 4 TMA, 5 MMA, 6 right-hand-side rows
 
-__global__ void __launch_bounds__(128, 1) k_gemm_half(const Prob* __restrict__ probs, int s) {
-  const Prob& P = probs[blockIdx.y];
-  const int ti = s + blockIdx.x;
-  if (P.mode != 1 || ti >= P.nt128 || P.status[1]) return;
-  extern __shared__ __align__(1024) unsigned char smh[];
-  uint64_t* full = reinterpret_cast<uint64_t*>(smh + 4 * STAGE);
-  uint64_t* done = full + 1;
-  uint32_t* slot = reinterpret_cast<uint32_t*>(full + 2);
-  __shared__ int s_ok;
-  const int tid = threadIdx.x, warp = tid >> 5;
+template <int NQ>
+__global__ void __launch_bounds__(CPL_THREADS, 1)
+    k_couple(const Prob* __restrict__ probs, int nprob, int s, int sq, int ns, int dq,
+             const int* __restrict__ prefix) {
+  constexpr int N = 32 * NQ;
+  constexpr uint32_t B_BYTES = NSLICE * 2 * N * 16;    // 7 planes x 2 k-groups x N rows x 16 B
+  constexpr uint32_t CSTAGE = A_STAGE + B_BYTES;
+  constexpr int NBUF = NQ == 1 ? 2 : 1;                 // TMEM buffers of 7 N columns
+  constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((128u >> 4) << 24);
+  extern __shared__ __align__(1024) unsigned char smq[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smq + CPL_NSTAGE * STAGE);
+  uint64_t* empty = full + CPL_NSTAGE;
+  uint64_t* tfull = full + 2 * CPL_NSTAGE;  // [2]
+  uint64_t* tempty = tfull + 2;             // [2]
+  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 4);
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nch = 2 * ns;
   if (tid == 0) {
-    s_ok = 1;
-    mbar_init(full, 1);
-    mbar_init(done, 1);
+    s_abort = 0;
+    for (int k = 0; k < CPL_NSTAGE; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], 1);
+    }
+    for (int k = 0; k < 2; ++k) {
+      mbar_init(&tfull[k], 1);
+      mbar_init(&tempty[k], 128);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_b) : "memory");
   }
-  if (warp == 0) {
+  if (warp == 5) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -488,84 +397,151 @@ __global__ void __launch_bounds__(128, 1) k_gemm_half(const Prob* __restrict__ p
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tbase = *slot;
-  if (tid == 0) {
-    mbar_expect_tx(full, 4 * STAGE);
-    for (int c = 0; c < 4; ++c) {
-      unsigned char* As = smh + c * STAGE;
-      tma_load_5d(As, P.tmap_a, 0, 0, 2 * c, 0, ti, full);
-      tma_load_5d(As + A_STAGE, P.tmap_b, 0, 2, 2 * c, 0, s, full);  // rows c0+64 .. c0+127
+  const int total = prefix[nprob];
+  auto decode = [&](int t, int& p, int& ti) {
+    int lo = 0, hi = nprob;  // largest p with prefix[p] <= t
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (prefix[mid] <= t) lo = mid; else hi = mid;
     }
-    bool ok = mbar_wait(full, 0);
-    if (ok) {
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint64_t adesc0 = smem_desc(su32(smh), 2048, 128);
-      const uint64_t bdesc0 = smem_desc(su32(smh) + A_STAGE, 1024, 128);
-      for (int c = 0; c < 4; ++c) {
-        const uint64_t soff = (uint64_t)((c * STAGE) >> 4);
-#pragma unroll
-        for (int pp = 0; pp < NSLICE; ++pp)
-#pragma unroll
-          for (int q = 0; q + pp < NSLICE; ++q)
-            mma_f16(tbase + (uint32_t)(pp + q) * 64, adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
-                    bdesc0 + soff + (uint64_t)(q * 2048 >> 4), (c == 0 && pp == 0) ? 0u : 1u);
-      }
-    }
-    mma_commit(done);
-    if (!ok) s_ok = 0;
-  }
-  const bool fin = mbar_wait(done, 0);
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  if (!fin || !s_ok) {
-    if (tid == 0) atomicExch(&P.status[2], 1);
-  } else {
-    const int c0 = s * NB;
-    const int i = ti * NB + tid;  // TMEM lane = tile row
-    const bool live = i >= c0 + 64 && i < P.Nc;
-    const double pi = P.pw2[i < P.Nc ? i : 0];
-    const size_t ld = (size_t)P.ld;
-    for (int g = 0; g < 8; ++g) {
-      uint32_t v[NSLICE][8];
-#pragma unroll
-      for (int l = 0; l < NSLICE; ++l)
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                     : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]), "=r"(v[l][5]),
-                       "=r"(v[l][6]), "=r"(v[l][7])
-                     : "r"(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * 64 + g * 8)));
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
-      if (live) {
-#pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          long long S[NSLICE];
-#pragma unroll
-          for (int l = 0; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
-          const long long low = S[4] * 65536 + S[5] * 256 + S[6];
-          const long long hi = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
-          const double w = fma((double)hi, 16777216.0, (double)(low & 0xFFFFFF));
-          const int j = c0 + 64 + g * 8 + jj;
-          double* kp = P.K + (size_t)j * ld + i;
-          *kp = *kp - w * pi * P.pw2[j];
+    p = lo;
+    ti = s + (t - prefix[lo]);
+  };
+
+  if (warp == 4) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      uint32_t g = 0;
+      for (int t = blockIdx.x; t < total && !s_abort; t += gridDim.x) {
+        int p, ti;
+        decode(t, p, ti);
+        const Prob& P = probs[p];
+        const void* tb = NQ == 1 ? P.tmap_b32 : P.tmap_b;
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tb) : "memory");
+        for (int c = 0; c < nch; ++c, ++g) {
+          const int st = g % CPL_NSTAGE;
+          if (!mbar_wait(&empty[st], ((g / CPL_NSTAGE) & 1) ^ 1)) {
+            s_abort = 1;
+            break;
+          }
+          unsigned char* As = smq + st * STAGE;
+          const int kg = 2 * (2 * sq + c);
+          mbar_expect_tx(&full[st], CSTAGE);
+          tma_load_5d(As, P.tmap_a, 0, 0, kg, 0, ti, &full[st]);
+          tma_load_5d(As + A_STAGE, tb, 0, dq, kg, 0, s, &full[st]);  // rows c0+32dq .. +N-1
         }
       }
     }
+  } else if (warp == 5) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      uint32_t g = 0, it = 0;
+      const uint64_t adesc0 = smem_desc(su32(smq), 2048, 128);
+      const uint64_t bdesc0 = smem_desc(su32(smq) + A_STAGE, N * 16, 128);
+      for (int t = blockIdx.x; t < total && !s_abort; t += gridDim.x, ++it) {
+        const int buf = it % NBUF;
+        const uint32_t use = it / NBUF;
+        if (!mbar_wait(&tempty[buf], (use & 1) ^ 1)) {
+          s_abort = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t dt = tbase + (uint32_t)buf * 256;
+        for (int c = 0; c < nch; ++c, ++g) {
+          const int st = g % CPL_NSTAGE;
+          if (!mbar_wait(&full[st], (g / CPL_NSTAGE) & 1)) {
+            s_abort = 1;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint64_t soff = (uint64_t)((st * STAGE) >> 4);
+#pragma unroll
+          for (int pp = 0; pp < NSLICE; ++pp)
+#pragma unroll
+            for (int qq = 0; qq + pp < NSLICE; ++qq)
+              mma_f16_desc(dt + (uint32_t)((pp + qq) * N), adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
+                           bdesc0 + soff + (uint64_t)((qq * 2 * N * 16) >> 4), IDESC, (c == 0 && pp == 0) ? 0u : 1u);
+          mma_commit(&empty[st]);
+        }
+        if (s_abort) break;
+        mma_commit(&tfull[buf]);
+      }
+    }
+  } else if (warp == 6) {
+    // ---------------- right-hand-side rows (FP64), problems round-robin ----------------
+    for (int p = blockIdx.x; p < nprob; p += gridDim.x) {
+      const Prob& P = probs[p];
+      if (P.mode != 1 || s >= P.nt128 || P.status[1]) continue;
+      const size_t ld = (size_t)P.ld;
+      const int c0 = s * NB;
+      for (int b = 0; b < P.nrhs; ++b) {
+        for (int jj = lane; jj < N; jj += 32) {
+          const int j = c0 + dq * QW + jj;
+          double a = 0.0;
+          for (int k = sq * QW; k < (sq + ns) * QW; ++k)
+            a = fma(P.K[(size_t)(c0 + k) * ld + P.Nc + b], P.K[(size_t)(c0 + k) * ld + j], a);
+          P.K[(size_t)j * ld + P.Nc + b] -= a;
+        }
+      }
+    }
+  } else {
+    // ---------------- epilogue (warps 0-3): row = TMEM lane ----------------
+    uint32_t it = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
+      int p, ti;
+      decode(t, p, ti);
+      const Prob& P = probs[p];
+      const int buf = it % NBUF;
+      const uint32_t use = it / NBUF;
+      if (!mbar_wait(&tfull[buf], use & 1)) {
+        s_abort = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int cd = s * NB + dq * QW;
+      const int i = ti * NB + tid;
+      const bool live = i >= cd && i < P.Nc;
+      const int ei = P.escale[i < P.Nc ? i : 0] - 62;
+      const size_t ld = (size_t)P.ld;
+      double* kcol = P.K + (size_t)cd * ld + i;
+#pragma unroll 1
+      for (int g = 0; g < N / 8; ++g) {
+        uint32_t v[NSLICE][8];
+#pragma unroll
+        for (int l = 0; l < NSLICE; ++l)
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                       : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
+                         "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
+                       : "r"(tbase + (uint32_t)buf * 256 + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * N + g * 8)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        if (live) {
+          double kv[8];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) kv[jj] = kcol[(size_t)(g * 8 + jj) * ld];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            long long S[NSLICE];
+#pragma unroll
+            for (int l = 0; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
+            const long long low = S[4] * 65536 + S[5] * 256 + S[6];
+            const long long hi = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
+            kv[jj] -= fixed_to_double(hi, (int)(low & 0xFFFFFF), ei + P.escale[cd + g * 8 + jj]);
+          }
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) kcol[(size_t)(g * 8 + jj) * ld] = kv[jj];
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      mbar_arrive(&tempty[buf]);
+    }
   }
-  asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
-}
-
-// the same coupling for the right-hand-side rows (FP64)
-__global__ void __launch_bounds__(128) k_border_half(const Prob* __restrict__ probs, int s) {
-  const Prob& P = probs[blockIdx.x];
-  if (P.mode != 1 || s >= P.nt128 || P.status[1]) return;
-  const int q = threadIdx.x >> 6, jj = threadIdx.x & 63;
-  if (q >= P.nrhs) return;
-  const size_t ld = (size_t)P.ld;
-  const int c0 = s * NB;
-  const int j = c0 + 64 + jj;
-  double a = 0.0;
-  for (int k = 0; k < 64; ++k) a = fma(P.K[(size_t)(c0 + k) * ld + P.Nc + q], P.K[(size_t)(c0 + k) * ld + j], a);
-  P.K[(size_t)j * ld + P.Nc + q] -= a;
+  if (s_abort && tid == 0) {
+    for (int k = 0; k < nprob; ++k) atomicExch(&probs[k].status[2], 1);
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == 5) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
 }
 
 // ---------------------------------------------------------------------------
@@ -620,6 +596,7 @@ int encode_slice_maps(void* host_maps, const void* slices, int nt128) {
   const cuuint64_t strides[4] = {512, 2048, (cuuint64_t)SLICE_BYTES, (cuuint64_t)NSLICE * SLICE_BYTES};
   const cuuint32_t boxA[5] = {256, 4, 2, NSLICE, 1};   // 128 rows
   const cuuint32_t boxB[5] = {256, 2, 2, NSLICE, 1};   // 64 rows
+  const cuuint32_t boxQ[5] = {256, 1, 2, NSLICE, 1};   // 32 rows
   const cuuint32_t es[5] = {1, 1, 1, 1, 1};
   CUtensorMap* m = static_cast<CUtensorMap*>(host_maps);
   CUresult r = fn(&m[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dims, strides, boxA, es,
@@ -629,6 +606,10 @@ int encode_slice_maps(void* host_maps, const void* slices, int nt128) {
   r = fn(&m[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dims, strides, boxB, es,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return (int)r;
+  r = fn(&m[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dims, strides, boxQ, es,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return (int)r;
 }
 
@@ -636,20 +617,16 @@ int encode_slice_maps(void* host_maps, const void* slices, int nt128) {
 // launch helpers
 // ---------------------------------------------------------------------------
 static bool g_attr = false;
-constexpr int TRSM128_SMEM = (NB * (NB + 1) + NB * (TB + 1) + NB) * (int)sizeof(double);
 static cudaError_t set_attrs() {
   if (g_attr) return cudaSuccess;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_potf2_128, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                NB * (NB + 1) * (int)sizeof(double))) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_trsm128, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                TRSM128_SMEM)) != cudaSuccess)
-    return e;
   if ((e = cudaFuncSetAttribute(k_ozaki_update, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM)) !=
       cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(k_gemm_half, cudaFuncAttributeMaxDynamicSharedMemorySize, HALF_SMEM)) !=
+  if ((e = cudaFuncSetAttribute(k_couple<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, CPL_SMEM)) !=
+      cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_couple<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, CPL_SMEM)) !=
       cudaSuccess)
     return e;
   g_attr = true;
@@ -668,47 +645,23 @@ cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc
   return cudaGetLastError();
 }
 
-cudaError_t launch_potf2_128(const Prob* probs, int nprob, int step, cudaStream_t s) {
-  cudaError_t e = set_attrs();
-  if (e != cudaSuccess) return e;
-  k_potf2_128<<<nprob, 512, NB * (NB + 1) * sizeof(double), s>>>(probs, step);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_trsm128(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
-  cudaError_t e = set_attrs();
-  if (e != cudaSuccess) return e;
-  const int tiles = 2 * max_nt128 + 1 - 2 * (step + 1);  // 64-row tiles below the block, incl. border
-  if (tiles <= 0) return cudaSuccess;
-  k_trsm128<<<dim3(tiles, nprob), 256, TRSM128_SMEM, s>>>(probs, step);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_split(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
-  const int m = max_nt128 - step - 1;
-  if (m <= 0) return cudaSuccess;
-  k_split<<<dim3(m, NB / 8, nprob), 128, 0, s>>>(probs, step, step + 1);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_split_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
+cudaError_t launch_split_quarter(const Prob* probs, int nprob, int step, int q, int max_nt128, cudaStream_t s) {
   const int m = max_nt128 - step;
   if (m <= 0) return cudaSuccess;
-  k_split<<<dim3(m, NB / 16, nprob), 128, 0, s>>>(probs, step, step);
+  k_split<<<dim3(m, QW / 8, nprob), 128, 0, s>>>(probs, step, step, q * (QW / 8));
   return cudaGetLastError();
 }
 
-cudaError_t launch_gemm_half(const Prob* probs, int nprob, int step, int max_nt128, cudaStream_t s) {
+cudaError_t launch_couple(const Prob* probs, int nprob, int step, int sq, int ns, int dq, int nq,
+                          const int* prefix, int total_tiles, int num_sms, cudaStream_t s) {
   cudaError_t e = set_attrs();
   if (e != cudaSuccess) return e;
-  const int m = max_nt128 - step;
-  if (m <= 0) return cudaSuccess;
-  k_gemm_half<<<dim3(m, nprob), 128, HALF_SMEM, s>>>(probs, step);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_border_half(const Prob* probs, int nprob, int step, cudaStream_t s) {
-  k_border_half<<<nprob, 128, 0, s>>>(probs, step);
+  int grid = total_tiles < num_sms ? total_tiles : num_sms;
+  if (grid < 1) grid = 1;  // the right-hand-side rows still need their coupling
+  if (nq == 1)
+    k_couple<1><<<grid, CPL_THREADS, CPL_SMEM, s>>>(probs, nprob, step, sq, ns, dq, prefix);
+  else
+    k_couple<2><<<grid, CPL_THREADS, CPL_SMEM, s>>>(probs, nprob, step, sq, ns, dq, prefix);
   return cudaGetLastError();
 }
 

@@ -65,6 +65,13 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b,
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
       "l"(a), "l"(b), "r"(IDESC_128x64), "r"(accumulate));
 }
+__device__ __forceinline__ void mma_f16_desc(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                             uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
                : "memory");
@@ -113,6 +120,35 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+
+// (hi 2^24 + lo) 2^e rounded to the nearest double (ties to even) with
+// integer operations only: |hi| < 2^62, 0 <= lo < 2^24.  The same double as
+// fma((double)hi, 2^24, (double)lo) scaled by 2^e, without the FP64 pipe.
+// Results below 2^-1022 (never reached by the factor's scales) flush to 0.
+__device__ __forceinline__ double fixed_to_double(long long hi, int lo, int e) {
+  const __int128 v = (__int128)hi * 16777216 + lo;
+  if (v == 0) return 0.0;
+  const bool neg = v < 0;
+  unsigned __int128 a = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const unsigned long long ah = (unsigned long long)(a >> 64), al = (unsigned long long)a;
+  const int lz = ah ? __clzll((long long)ah) : 64 + __clzll((long long)al);
+  a <<= lz;  // leading one at bit 127
+  const unsigned long long top = (unsigned long long)(a >> 64);
+  const bool sticky = (unsigned long long)a != 0;
+  unsigned long long mant = top >> 11;  // 53 bits
+  const unsigned long long rb = top & 0x7FF;
+  if (rb > 0x400 || (rb == 0x400 && (sticky || (mant & 1)))) ++mant;
+  int E = 127 - lz + e;  // value = 1.f 2^E
+  if (mant >> 53) {
+    mant >>= 1;
+    ++E;
+  }
+  const int be = E + 1023;
+  if (be <= 0) return neg ? -0.0 : 0.0;
+  if (be >= 2047) return __longlong_as_double(neg ? (long long)0xFFF0000000000000ULL : 0x7FF0000000000000LL);
+  return __longlong_as_double((long long)(((unsigned long long)neg << 63) | ((unsigned long long)be << 52) |
+                                          (mant & 0xFFFFFFFFFFFFFULL)));
 }
 
 // tile t of step s -> (problem, 128-row tile, 64-column tile); false if out of range

@@ -123,12 +123,12 @@ class Plan:
     def set_profiling(self, enable=True):
         _lib.check(self.lib.fgpu_plan_set_profiling(self.handle, 1 if enable else 0))
 
-    STAGES = ("build", "potf2", "trsm", "update", "finalize", "panel_prep", "split", "border")
+    STAGES = ("build", "potf2", "trsm", "update", "finalize", "panel_prep", "split", "border", "coupling")
 
     def stage_times(self):
         """{stage: (ms during the last replay, launches)}."""
-        ms = np.zeros(8)
-        cnt = np.zeros(8, dtype=np.int32)
+        ms = np.zeros(len(self.STAGES))  # FGPU_NSTAGES entries
+        cnt = np.zeros(len(self.STAGES), dtype=np.int32)
         _lib.check(self.lib.fgpu_plan_stage_times(self.handle, _dp(ms), cnt.ctypes.data_as(_lib.c_int_p)))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.STAGES)}
 

@@ -151,10 +151,10 @@ int fgpu_loglik_noalloc(int N, int d, const double* X_dev, const double* y_dev, 
  * fgpu_plan_stage_times fills ms[k] with the summed device time of stage k
  * during the LAST replay and count[k] with its launches (k: 0 build,
  * 1 diagonal factor, 2 panel solve, 3 trailing update, 4 likelihood
- * epilogue, 5 panel conversion, 6 digit split and half-panel coupling,
- * 7 right-hand-side rows).
+ * epilogue, 5 panel conversion, 6 digit split, 7 right-hand-side rows,
+ * 8 quarter-panel coupling).
  * Diagnostic only; the reference has no counterpart. */
-#define FGPU_NSTAGES 8
+#define FGPU_NSTAGES 9
 int fgpu_plan_set_profiling(fgpu_plan* plan, int enable);
 int fgpu_plan_stage_times(fgpu_plan* plan, double* ms, int* count);
 
