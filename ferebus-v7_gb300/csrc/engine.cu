@@ -580,6 +580,50 @@ __global__ void __launch_bounds__(256) k_trsmw(const Prob* __restrict__ probs, i
 }
 
 // ---------------------------------------------------------------------------
+// the same solve with one thread per row: row r of the panel, x (1 x W), is
+// x L11^T = b, i.e. forward substitution x_c = (b_c - sum_{k<c} x_k L_ck) / L_cc,
+// independent for every row.  The row stays in registers and L11 is read
+// from shared memory by all threads at once (broadcast): no block barrier
+// inside the solve.  128 rows per CTA.
+// ---------------------------------------------------------------------------
+template <int W>
+__global__ void __launch_bounds__(128) k_trsm_rows(const Prob* __restrict__ probs, int col0_step, int col0_off) {
+  const Prob& P = probs[blockIdx.y];
+  const int col0 = col0_step + col0_off;
+  const int last = P.nrt ? P.nrt - 1 : P.nsteps;  // last 64-row tile
+  const int row_end = (last + 1) * TB;
+  const int rbase = col0 + W + blockIdx.x * 128;
+  if (col0 >= P.Nc || rbase >= row_end) return;
+  if (*(volatile int*)&P.status[1]) return;
+  __shared__ double L[W * W];  // L[c * W + k] = L_ck (row c, column k), lower
+  __shared__ double rd[W];
+  const size_t ld = (size_t)P.ld;
+  const double* Ld = P.K + (size_t)col0 * ld + col0;
+  for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+    const int c = e % W, k = e / W;  // column k, row c: coalesced over c
+    L[c * W + k] = Ld[(size_t)k * ld + c];
+  }
+  __syncthreads();
+  if (threadIdx.x < W) rd[threadIdx.x] = 1.0 / L[threadIdx.x * W + threadIdx.x];
+  __syncthreads();
+  const int r = rbase + threadIdx.x;
+  if (r >= row_end) return;
+  double* row = P.K + (size_t)col0 * ld + r;
+  double x[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) x[c] = row[(size_t)c * ld];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    double a = x[c];
+#pragma unroll
+    for (int k = 0; k < c; ++k) a = fma(-x[k], L[c * W + k], a);
+    x[c] = a * rd[c];
+  }
+#pragma unroll
+  for (int c = 0; c < W; ++c) row[(size_t)c * ld] = x[c];
+}
+
+// ---------------------------------------------------------------------------
 // trailing update C(ti, tj) -= P(ti) P(tj)^T on the FP64 MMA pipe
 // (mma.sync m8n8k4 f64).  128 threads, 4 warps x (32 x 32).
 // ---------------------------------------------------------------------------
@@ -821,7 +865,7 @@ cudaError_t launch_potf2_quarter(const Prob* probs, int nprob, int step, int q, 
 cudaError_t launch_trsm_quarter(const Prob* probs, int nprob, int step, int q, int max_rows, cudaStream_t s) {
   const int rows = max_rows - (step * NB + q * QW + QW);
   if (rows <= 0) return cudaSuccess;
-  k_trsmw<QW><<<dim3((rows + TB - 1) / TB, nprob), 256, 0, s>>>(probs, step * NB, q * QW);
+  k_trsm_rows<QW><<<dim3((rows + 127) / 128, nprob), 128, 0, s>>>(probs, step * NB, q * QW);
   return cudaGetLastError();
 }
 
