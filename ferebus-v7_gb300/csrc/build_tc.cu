@@ -30,7 +30,8 @@
 // multilinear in the (at most two) distance leaves: k = a + b v0 + c v1 +
 // d v0 v1, with a..d from the constant / linear leaves (one thread per
 // problem, before the build).  The persistent kernel has the update's
-// structure: TMA producer warp, MMA warp, 8 epilogue warps; one pass per
+// structure: TMA producer warp, MMA warp, 16 epilogue warps (the epilogue's
+// integer work is what bounds the kernel, so it gets the warps); one pass per
 // distance leaf per 128 x 64 tile.
 #include "../../include/fgpu.h"
 #include "fgpu_internal.h"
@@ -168,7 +169,8 @@ __global__ void __launch_bounds__(128) k_feat_digits(const Prob* __restrict__ pr
 // ---------------------------------------------------------------------------
 // persistent tensor-core build of the lower triangle (128 x 64 tiles)
 // ---------------------------------------------------------------------------
-constexpr int BLD_THREADS = 320;
+constexpr int BLD_EPI_WARPS = 16;                      // 4 lane quarters x 4 groups of 16 columns
+constexpr int BLD_THREADS = (BLD_EPI_WARPS + 2) * 32;  // + TMA warp + MMA warp
 constexpr int NSTAGE = 3;
 constexpr uint32_t BLD_SMEM = NSTAGE * STAGE + 256;
 
@@ -189,10 +191,10 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
       mbar_init(&empty[k], 1);
     }
     mbar_init(tfull, 1);
-    mbar_init(tempty, 256);
+    mbar_init(tempty, BLD_EPI_WARPS * 32);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 9) {
+  if (warp == BLD_EPI_WARPS + 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -202,7 +204,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
   const uint32_t tbase = *slot;
   const int total = prefix[nprob];
 
-  if (warp == 8) {
+  if (warp == BLD_EPI_WARPS) {
     // ---------------- TMA producer: digit planes of each leaf's k chunks ----------------
     if (lane == 0) {
       uint32_t g = 0;
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
         }
       }
     }
-  } else if (warp == 9) {
+  } else if (warp == BLD_EPI_WARPS + 1) {
     // ---------------- MMA issuer: one pass of 35 pairs per chunk per leaf ----------------
     if (lane == 0) {
       uint32_t g = 0, it = 0;
@@ -272,9 +274,9 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
       }
     }
   } else {
-    // ---------------- epilogue (warps 0-7) ----------------
+    // ---------------- epilogue (warps 0-15) ----------------
     const int r = (warp & 3) * 32 + lane;  // TMEM lane = tile row
-    const int h = warp >> 2;               // column half
+    const int h = warp >> 2;               // group of 16 columns
     const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
     uint32_t it = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
@@ -284,8 +286,8 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
       const Spec& sp = *P.spec;
       const size_t nc = (size_t)P.Nc;
       const int i = ti * NB + r;
-      const int j0 = tj * TB + h * 32;
-      double v0[32];
+      const int j0 = tj * TB + h * 16;
+      double v0[16];
       bool stop = false;
       for (int d = 0; d < sp.ndot; ++d, ++it) {
         if (!mbar_wait(tfull, it & 1)) {
@@ -294,17 +296,17 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        long long W[32];
+        long long W[16];
         const int u = sp.dot_u[d];
 #pragma unroll
-        for (int gq = 0; gq < 4; ++gq) {
+        for (int gq = 0; gq < 2; ++gq) {
           uint32_t v[NLEV][8];
 #pragma unroll
           for (int l = 0; l < NLEV; ++l) {
             asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                          : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
                            "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
-                         : "r"(tbase + lane_base + (uint32_t)(l * 64 + h * 32 + gq * 8)));
+                         : "r"(tbase + lane_base + (uint32_t)(l * 64 + h * 16 + gq * 8)));
           }
           asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
@@ -322,7 +324,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
         const long long wi = P.fnorm[(size_t)d * nc + i];
         const long long* wj = P.fnorm + (size_t)d * nc + j0;
 #pragma unroll
-        for (int q = 0; q < 32; ++q) {
+        for (int q = 0; q < 16; ++q) {
           long long E = wi + wj[q] - 2 * W[q];
           E = E < 0 ? 0 : E;
           const double val = iexp_fixed((unsigned long long)E, eexp);
@@ -339,7 +341,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
       double* K = P.K;
       const size_t ld = (size_t)P.ld;
 #pragma unroll
-      for (int q = 0; q < 32; ++q) {
+      for (int q = 0; q < 16; ++q) {
         const int j = j0 + q;
         double val = sp.ndot == 1 ? fma(P.fcoef[1], v0[q], P.fcoef[0]) : v0[q];
         if (j > i) val = 0.0;
@@ -354,7 +356,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
     for (int q = 0; q < nprob; ++q) atomicExch(&probs[q].status[2], 1);
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
-  if (warp == 9) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
+  if (warp == BLD_EPI_WARPS + 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
 }
 
 // ---------------------------------------------------------------------------
