@@ -398,9 +398,9 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
     const int max_rows = max_nc + TB;  // the tallest problem's ld: factor rows + right-hand sides
     for (int step = 0; step < nt; ++step) {
       if (step > 0) STAGE(5, launch_panel_prep(probs_d, nprob, step, max_nc, s));
-      // four 32-column quarters: FP64 diagonal factor, panel solve and digit
-      // planes of each; tensor-core couplings quarter 0 -> 1, half 0 -> 1,
-      // quarter 2 -> 3 before the quarter that needs them
+      // four 32-column quarters: FP64 diagonal factor, panel solve (which
+      // writes the quarter's digit planes); tensor-core couplings quarter
+      // 0 -> 1, half 0 -> 1, quarter 2 -> 3 before the quarter that needs them
       const int* rows_prefix = us->row_prefix_dev + (size_t)step * us->stride;
       const int rows_total = us->row_totals[step];
       for (int q = 0; q < NB / QW; ++q) {
@@ -408,8 +408,7 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
         if (q == 2) STAGE(8, launch_couple(probs_d, nprob, step, 0, 2, 2, 2, rows_prefix, rows_total, us->num_sms, s));
         if (q == 3) STAGE(8, launch_couple(probs_d, nprob, step, 2, 1, 3, 1, rows_prefix, rows_total, us->num_sms, s));
         STAGE(1, launch_potf2_quarter(probs_d, nprob, step, q, s));
-        STAGE(2, launch_trsm_quarter(probs_d, nprob, step, q, max_rows, s));
-        STAGE(6, launch_split_quarter(probs_d, nprob, step, q, nt, s));
+        STAGE(2, launch_trsm_quarter(probs_d, nprob, step, q, max_rows, s));  // also its digit planes
       }
       if (step + 1 < nt) {
         STAGE(3, launch_ozaki_update(probs_d, nprob, step, nt, us->prefix_dev + (size_t)step * us->stride,

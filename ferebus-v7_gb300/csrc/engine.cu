@@ -8,6 +8,7 @@
 #include "../../include/fgpu.h"
 #include "fgpu_internal.h"
 #include "iexp.cuh"
+#include "tc_common.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -17,42 +18,6 @@ namespace fgpu {
 #define FGPU_PI 3.141592653589793115997963468544185161590576171875
 #define FGPU_TWOPI 6.28318530717958623199592693708837032318115234375
 #define FGPU_LOG_TWOPI 1.8378770664093453390819377091247588396072387695312
-
-// ---------------------------------------------------------------------------
-// small PTX helpers: mbarrier + bulk async copy (the TMA engine's 1-D form)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: returns false if the barrier did not complete within the limit.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (int it = 0; it < (1 << 22); ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
 
 // ---------------------------------------------------------------------------
 // kernel-matrix build
@@ -182,7 +147,7 @@ __global__ void __launch_bounds__(256) k_build(const Prob* __restrict__ probs) {
   if (tid == 0 && np > 0) {
     const uint32_t per = TB * sizeof(double);
     const uint32_t total = per * np * (border ? 1 : 2);
-    mbar_arrive_expect_tx(bar, total);
+    mbar_expect_tx(bar, total);
     for (int p = 0; p < np; ++p) {
       bulk_g2s(Pj + p * TB, P.planes + (size_t)p * P.Nc + j0, per, bar);
       if (!border) bulk_g2s(Pi + p * TB, P.planes + (size_t)p * P.Nc + i0, per, bar);
@@ -205,7 +170,7 @@ __global__ void __launch_bounds__(256) k_build(const Prob* __restrict__ probs) {
       for (int k = 0; k < L.n; ++k) s += 1.0 / ls[L.param0 + k];
     lin_sums[tid] = s;
   }
-  if (np > 0 && !mbar_wait_bounded(bar, 0)) s_fail = 1;
+  if (np > 0 && !mbar_wait(bar, 0)) s_fail = 1;
   __syncthreads();
   if (s_fail) {
     if (tid == 0) atomicExch(&P.status[2], 1);  // copy engine did not answer: report, do not hang
@@ -326,7 +291,7 @@ __global__ void __launch_bounds__(256) k_build_dot(const Prob* __restrict__ prob
   if (tid == 0) {
     const uint32_t per = TB * sizeof(double);
     const uint32_t nrows = (uint32_t)(np + nl);
-    mbar_arrive_expect_tx(bar, per * nrows * (border ? 1 : 2));
+    mbar_expect_tx(bar, per * nrows * (border ? 1 : 2));
     for (int p = 0; p < np; ++p) {
       bulk_g2s(Pj + p * TB, P.splanes + (size_t)p * nc + j0, per, bar);
       if (!border) bulk_g2s(Pi + p * TB, P.splanes + (size_t)p * nc + i0, per, bar);
@@ -354,7 +319,7 @@ __global__ void __launch_bounds__(256) k_build_dot(const Prob* __restrict__ prob
       for (int k = 0; k < L.n; ++k) acc += ls[L.param0 + k];
     leaf_c[tid] = acc;
   }
-  if (!mbar_wait_bounded(bar, 0)) s_fail = 1;
+  if (!mbar_wait(bar, 0)) s_fail = 1;
   __syncthreads();
   if (s_fail) {
     if (tid == 0) atomicExch(&P.status[2], 1);
@@ -584,7 +549,11 @@ __global__ void __launch_bounds__(256) k_trsmw(const Prob* __restrict__ probs, i
 // x L11^T = b, i.e. forward substitution x_c = (b_c - sum_{k<c} x_k L_ck) / L_cc,
 // independent for every row.  The row stays in registers and L11 is read
 // from shared memory by all threads at once (broadcast): no block barrier
-// inside the solve.  128 rows per CTA.
+// inside the solve.  128 rows per CTA.  In tensor-core mode the thread also
+// writes the 7 fp16 digit planes of its finished row segment (factor rows
+// r < Nc), which is everything the couplings and the trailing update read
+// of this quarter: their live rows and B rows all lie below the quarter's
+// diagonal block.
 // ---------------------------------------------------------------------------
 template <int W>
 __global__ void __launch_bounds__(128) k_trsm_rows(const Prob* __restrict__ probs, int col0_step, int col0_off) {
@@ -621,6 +590,37 @@ __global__ void __launch_bounds__(128) k_trsm_rows(const Prob* __restrict__ prob
   }
 #pragma unroll
   for (int c = 0; c < W; ++c) row[(size_t)c * ld] = x[c];
+  if (P.mode == 1 && r < P.Nc) {
+    // digit planes, layout [row tile][plane][k-group of 8][row][8 x fp16]
+    const int e = P.escale[r];
+    bool bad = false;
+    unsigned char* base = P.slices + (size_t)(r / NB) * NSLICE * SLICE_BYTES + (size_t)(r % NB) * 16;
+    const int kg0 = (col0 % NB) / 8;
+#pragma unroll
+    for (int g = 0; g < W / 8; ++g) {
+      int d[NSLICE][8];
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        long long F = to_fixed55(x[g * 8 + kk], e, &bad);
+#pragma unroll
+        for (int p = NSLICE - 1; p >= 1; --p) {
+          const int b = (int)(signed char)(F & 0xFF);
+          d[p][kk] = b;
+          F = (F - b) >> 8;
+        }
+        d[0][kk] = (int)F;
+      }
+#pragma unroll
+      for (int p = 0; p < NSLICE; ++p) {
+        __align__(16) __half h[8];
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) h[kk] = __int2half_rn(d[p][kk]);
+        *reinterpret_cast<uint4*>(base + (size_t)p * SLICE_BYTES + (size_t)(kg0 + g) * 2048) =
+            *reinterpret_cast<const uint4*>(h);
+      }
+    }
+    if (bad) atomicOr(&P.status[3], 1);
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -112,7 +112,8 @@ cudaError_t launch_build_dot(const Prob* probs, int nprob, int max_nsteps, int m
 size_t build_dot_smem_bytes(int nplanes);
 cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s);
 // tensor-core mode: the 32 x 32 diagonal block of quarter q of panel step, and
-// the rows below it up to max_rows (the tallest problem's ld)
+// the rows below it up to max_rows (the tallest problem's ld), which also
+// writes their fp16 digit planes
 constexpr int QW = 32;
 cudaError_t launch_potf2_quarter(const Prob* probs, int nprob, int step, int q, cudaStream_t s);
 cudaError_t launch_trsm_quarter(const Prob* probs, int nprob, int step, int q, int max_rows, cudaStream_t s);
@@ -137,12 +138,11 @@ cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc
 cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, const int* prefix,
                                 int total_tiles, int num_sms, cudaStream_t s);
 cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
-// four 32-column quarters per 128-panel: digit planes of quarter q (rows from
-// the panel's own row tile), and the tensor-core coupling of source quarters
+// four 32-column quarters per 128-panel (their digit planes are written by
+// the quarter panel solve): the tensor-core coupling of source quarters
 // [sq, sq + ns) into destination quarters [dq, dq + nq), nq = 1 or 2 (with
 // the right-hand-side rows in FP64).  prefix: nprob + 1 offsets of the row
 // tiles ti >= step of each problem.
-cudaError_t launch_split_quarter(const Prob* probs, int nprob, int step, int q, int max_nt128, cudaStream_t s);
 cudaError_t launch_couple(const Prob* probs, int nprob, int step, int sq, int ns, int dq, int nq,
                           const int* prefix, int total_tiles, int num_sms, cudaStream_t s);
 

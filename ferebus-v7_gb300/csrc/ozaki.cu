@@ -76,43 +76,6 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
 }
 
 // ---------------------------------------------------------------------------
-// digit planes of panel s, k-groups kg0.. (8 columns each), for the rows of
-// 128-row tiles ti0..; layout per 128-row tile and digit p:
-// [kgroup 16][row 128][8 k] fp16
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_split(const Prob* __restrict__ probs, int s, int ti0, int kg0) {
-  const Prob& P = probs[blockIdx.z];
-  const int ti = ti0 + blockIdx.x;
-  if (P.mode != 1 || ti >= P.nt128 || P.status[1]) return;
-  const int r = threadIdx.x, kg = kg0 + blockIdx.y;
-  const int i = ti * NB + r;
-  const int e = P.escale[i];
-  const size_t ld = (size_t)P.ld;
-  const double* col = P.K + (size_t)(s * NB + kg * 8) * ld + i;
-  int d[NSLICE][8];
-  bool bad = false;
-  for (int kk = 0; kk < 8; ++kk) {
-    // only the lower triangle belongs to the factor (rows of the panel's own
-    // diagonal block carry stale values above the diagonal)
-    const double x = (s * NB + kg * 8 + kk > i) ? 0.0 : col[(size_t)kk * ld];
-    long long F = to_fixed55(x, e, &bad);
-    for (int p = NSLICE - 1; p >= 1; --p) {
-      const int b = (int)(signed char)(F & 0xFF);
-      d[p][kk] = b;
-      F = (F - b) >> 8;
-    }
-    d[0][kk] = (int)F;
-  }
-  if (bad) atomicOr(&P.status[3], 1);
-  unsigned char* base = P.slices + (size_t)ti * NSLICE * SLICE_BYTES + (size_t)kg * 2048 + (size_t)r * 16;
-  for (int p = 0; p < NSLICE; ++p) {
-    __align__(16) __half h[8];
-    for (int kk = 0; kk < 8; ++kk) h[kk] = __int2half_rn(d[p][kk]);
-    *reinterpret_cast<uint4*>(base + (size_t)p * SLICE_BYTES) = *reinterpret_cast<const uint4*>(h);
-  }
-}
-
-// ---------------------------------------------------------------------------
 // trailing update of the integer accumulators: persistent, warp-specialised
 //
 // Output tiles are 128 rows x 64 columns; a tile's 7 level sums occupy 448
@@ -642,13 +605,6 @@ cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc
   const int rows = max_nc - step * NB;
   if (step == 0 || rows <= 0) return cudaSuccess;
   k_panel_prep<<<dim3((rows + 255) / 256, NB / 16, nprob), 256, 0, s>>>(probs, step);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_split_quarter(const Prob* probs, int nprob, int step, int q, int max_nt128, cudaStream_t s) {
-  const int m = max_nt128 - step;
-  if (m <= 0) return cudaSuccess;
-  k_split<<<dim3(m, QW / 8, nprob), 128, 0, s>>>(probs, step, step, q * (QW / 8));
   return cudaGetLastError();
 }
 
