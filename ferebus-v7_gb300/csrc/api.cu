@@ -147,6 +147,10 @@ struct UpdSched {
   int build_total = 0;
   int* row_prefix_dev = nullptr;    // per step, nprob + 1: 128-row tiles ti >= step (quarter coupling)
   std::vector<int> row_totals;
+  int* cpl_order_dev = nullptr;     // per step: (problem << 16 | ti) of its row tiles, own row tile first
+  std::vector<size_t> cpl_off;      // offset of each step's order
+  int* cpl_counter_dev = nullptr;   // per step x 3 couplings: tile counters, zeroed per evaluation
+  int ncounters = 0;
 };
 
 struct Workspace {
@@ -346,6 +350,24 @@ int build_sched(const std::vector<int>& nt128, const std::vector<int>& tc_build,
     CK(cudaMalloc(&u.row_prefix_dev, sizeof(int) * r.size()));
     if (track) track->push_back(u.row_prefix_dev);
     CK(cudaMemcpy(u.row_prefix_dev, r.data(), sizeof(int) * r.size(), cudaMemcpyHostToDevice));
+    // dynamic order of the couplings' tiles: every problem's own row tile
+    // (which also carries the next quarter's diagonal factor) first
+    std::vector<int> ord;
+    u.cpl_off.assign(std::max(ntmax, 1), 0);
+    for (int st = 0; st < ntmax; ++st) {
+      u.cpl_off[st] = ord.size();
+      for (int p = 0; p < nprob; ++p)
+        if (nt128[p] > st) ord.push_back((p << 16) | st);
+      for (int p = 0; p < nprob; ++p)
+        for (int ti = st + 1; ti < nt128[p]; ++ti) ord.push_back((p << 16) | ti);
+    }
+    if (ord.empty()) ord.push_back(0);
+    CK(cudaMalloc(&u.cpl_order_dev, sizeof(int) * ord.size()));
+    if (track) track->push_back(u.cpl_order_dev);
+    CK(cudaMemcpy(u.cpl_order_dev, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
+    u.ncounters = 3 * std::max(ntmax, 1);
+    CK(cudaMalloc(&u.cpl_counter_dev, sizeof(int) * u.ncounters));
+    if (track) track->push_back(u.cpl_counter_dev);
   }
   // tensor-core build: the whole lower triangle, nt128 (nt128 + 1) tiles of 128 x 64
   std::vector<int> b(nprob + 1, 0);
@@ -387,6 +409,7 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
   if (mode == 1) {
     // 128-wide panels; max_nsteps counts 64-column tiles
     const int nt = max_nsteps / 2, max_nc = max_nsteps * TB;
+    CK(cudaMemsetAsync(us->cpl_counter_dev, 0, sizeof(int) * us->ncounters, s));
     STAGE(0, launch_prep_planes(probs_d, nprob, max_nc, s));
     if (us->build_total > 0) STAGE(0, launch_feat_digits(probs_d, nprob, nt, s));
     // FP64 dot-product build: every tile of the other problems, the
@@ -400,14 +423,16 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
       if (step > 0) STAGE(5, launch_panel_prep(probs_d, nprob, step, max_nc, s));
       // four 32-column quarters: FP64 diagonal factor, panel solve (which
       // writes the quarter's digit planes); tensor-core couplings quarter
-      // 0 -> 1, half 0 -> 1, quarter 2 -> 3 before the quarter that needs them
-      const int* rows_prefix = us->row_prefix_dev + (size_t)step * us->stride;
+      // 0 -> 1, half 0 -> 1, quarter 2 -> 3 before the quarter that needs
+      // them, each of which also factors that quarter's diagonal block
+      const int* order = us->cpl_order_dev + us->cpl_off[step];
       const int rows_total = us->row_totals[step];
+      int* ctr = us->cpl_counter_dev + 3 * step;
       for (int q = 0; q < NB / QW; ++q) {
-        if (q == 1) STAGE(8, launch_couple(probs_d, nprob, step, 0, 1, 1, 1, rows_prefix, rows_total, us->num_sms, s));
-        if (q == 2) STAGE(8, launch_couple(probs_d, nprob, step, 0, 2, 2, 2, rows_prefix, rows_total, us->num_sms, s));
-        if (q == 3) STAGE(8, launch_couple(probs_d, nprob, step, 2, 1, 3, 1, rows_prefix, rows_total, us->num_sms, s));
-        STAGE(1, launch_potf2_quarter(probs_d, nprob, step, q, s));
+        if (q == 1) STAGE(8, launch_couple(probs_d, nprob, step, 0, 1, 1, 1, order, rows_total, ctr, us->num_sms, s));
+        if (q == 2) STAGE(8, launch_couple(probs_d, nprob, step, 0, 2, 2, 2, order, rows_total, ctr + 1, us->num_sms, s));
+        if (q == 3) STAGE(8, launch_couple(probs_d, nprob, step, 2, 1, 3, 1, order, rows_total, ctr + 2, us->num_sms, s));
+        if (q == 0) STAGE(1, launch_potf2_quarter(probs_d, nprob, step, q, s));  // q > 0: inside the coupling
         STAGE(2, launch_trsm_quarter(probs_d, nprob, step, q, max_rows, s));  // also its digit planes
       }
       if (step + 1 < nt) {
@@ -509,6 +534,8 @@ void free_worker(Worker* w) {
   cudaFree(w->sched.prefix_dev);
   cudaFree(w->sched.build_prefix_dev);
   cudaFree(w->sched.row_prefix_dev);
+  cudaFree(w->sched.cpl_order_dev);
+  cudaFree(w->sched.cpl_counter_dev);
   if (w->h_stage) cudaFreeHost(w->h_stage);
   if (w->stream) cudaStreamDestroy(w->stream);
   delete w;

@@ -9,6 +9,7 @@
 #include "fgpu_internal.h"
 #include "iexp.cuh"
 #include "tc_common.cuh"
+#include "potf2_block.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -388,110 +389,12 @@ __global__ void __launch_bounds__(256) k_build_dot(const Prob* __restrict__ prob
 template <int W>
 __global__ void __launch_bounds__(W * 4) k_potf2w(const Prob* __restrict__ probs, int col0_step, int col0_off,
                                                   int part_step, int part_off) {
-  // Blocked left-looking factorisation in shared memory, panels of 8
-  // columns (the dot-product order of LAPACK's dpotf2, lapack/dpotf2.f):
-  // (a) the panel minus the finished columns times their rows, all threads;
-  // (b) the 8 x 8 diagonal block by one warp in registers (shuffles, no
-  // block barriers); (c) the rows below by forward substitution, one thread
-  // per row.  Three block barriers per panel.
   const Prob& P = probs[blockIdx.x];
   const int col0 = col0_step + col0_off;
   if (col0 >= P.Nc) return;
   if (*(volatile int*)&P.status[1]) return;
-  constexpr int LDA = W + 1;
-  __shared__ double A[W * LDA];  // A[c * LDA + r]
-  __shared__ double rdg[W];      // 1 / L_cc
-  __shared__ int fail_col;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const size_t ld = (size_t)P.ld;
-  double* Kd = P.K + (size_t)col0 * ld + col0;
-  for (int e = tid; e < W * W; e += blockDim.x) {
-    const int r = e % W, c = e / W;
-    A[c * LDA + r] = Kd[(size_t)c * ld + r];
-  }
-  if (tid == 0) fail_col = -1;
-  __syncthreads();
-  for (int c0 = 0; c0 < W; c0 += 8) {
-    // (a) columns c0..c0+7, rows >= column: subtract sum_{k < c0} L_rk L_ck
-    if (c0 > 0) {
-      const int r = tid % W, cp = c0 + 2 * (tid / W);
-      if (r >= cp) {
-        double a0 = A[cp * LDA + r], a1 = A[(cp + 1) * LDA + r];
-        for (int k = 0; k < c0; ++k) {
-          const double l = A[k * LDA + r];
-          a0 = fma(-l, A[k * LDA + cp], a0);
-          a1 = fma(-l, A[k * LDA + cp + 1], a1);
-        }
-        A[cp * LDA + r] = a0;
-        if (r > cp) A[(cp + 1) * LDA + r] = a1;
-      }
-    }
-    __syncthreads();
-    // (b) 8 x 8 diagonal block: lane i < 8 holds row c0 + i
-    if (warp == 0) {
-      double v[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] = (lane < 8 && k <= lane) ? A[(c0 + k) * LDA + c0 + lane] : 0.0;
-#pragma unroll
-      for (int jj = 0; jj < 8; ++jj) {
-        const double d = __shfl_sync(0xffffffffu, v[jj], jj);
-        if (!(d > 0.0)) {  // d is the same in every lane: the warp leaves together
-          if (lane == 0) fail_col = c0 + jj;
-          break;
-        }
-        const double sd = sqrt(d);
-        const double rd = 1.0 / sd;
-        if (lane == jj) v[jj] = sd;
-        if (lane > jj) v[jj] *= rd;
-#pragma unroll
-        for (int c = jj + 1; c < 8; ++c) {
-          const double lcj = __shfl_sync(0xffffffffu, v[jj], c);
-          if (lane >= c) v[c] = fma(-v[jj], lcj, v[c]);
-        }
-        if (lane == 0) rdg[c0 + jj] = rd;
-      }
-      if (lane < 8) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-          if (k <= lane) A[(c0 + k) * LDA + c0 + lane] = v[k];
-      }
-    }
-    __syncthreads();
-    if (fail_col >= 0) break;
-    // (c) rows below the diagonal block: forward substitution over the panel
-    if (tid < W - c0 - 8) {
-      const int r = c0 + 8 + tid;
-      double x[8];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        double a = A[(c0 + c) * LDA + r];
-#pragma unroll
-        for (int k = 0; k < c; ++k) a = fma(-x[k], A[(c0 + k) * LDA + c0 + c], a);
-        x[c] = a * rdg[c0 + c];
-        A[(c0 + c) * LDA + r] = x[c];
-      }
-    }
-    __syncthreads();
-  }
-  if (fail_col >= 0) {
-    if (tid == 0) {
-      P.status[0] = col0 + fail_col + 1;  // LAPACK info: 1-based column
-      P.status[1] = 1;
-    }
-    return;
-  }
-  for (int e = tid; e < W * W; e += blockDim.x) {
-    const int r = e % W, c = e / W;
-    if (r >= c) Kd[(size_t)c * ld + r] = A[c * LDA + r];
-  }
-  // log-det partial: 2 * sum log(L_jj) is formed in the epilogue
-  // (arith.f90:72-93); here the block's sum of logs, in column order.
-  if (tid < 32) {
-    double sl = 0.0;
-    for (int c = tid * (W / 32); c < (tid + 1) * (W / 32); ++c) sl += log(A[c * LDA + c]);
-    for (int o = 16; o > 0; o >>= 1) sl += __shfl_down_sync(0xffffffffu, sl, o);
-    if (tid == 0) P.logdet_part[part_step + part_off] = sl;
-  }
+  __shared__ PotfShared<W> sh;
+  potf2_block<W>(P, col0, part_step + part_off, threadIdx.x, sh, 0);
 }
 
 // ---------------------------------------------------------------------------

@@ -141,10 +141,12 @@ cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max
 // four 32-column quarters per 128-panel (their digit planes are written by
 // the quarter panel solve): the tensor-core coupling of source quarters
 // [sq, sq + ns) into destination quarters [dq, dq + nq), nq = 1 or 2 (with
-// the right-hand-side rows in FP64).  prefix: nprob + 1 offsets of the row
-// tiles ti >= step of each problem.
+// the right-hand-side rows in FP64), which also factors quarter dq's
+// diagonal block.  order: the step's total_tiles row tiles as
+// (problem << 16 | ti), each problem's own row tile first; counter: a zeroed
+// int the CTAs take tiles from.
 cudaError_t launch_couple(const Prob* probs, int nprob, int step, int sq, int ns, int dq, int nq,
-                          const int* prefix, int total_tiles, int num_sms, cudaStream_t s);
+                          const int* order, int total_tiles, int* counter, int num_sms, cudaStream_t s);
 
 // Tensor-core kernel-matrix build (build_tc.cu): feature digit planes and
 // exact self products, then the persistent build of the lower triangle.

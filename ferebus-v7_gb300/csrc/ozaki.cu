@@ -27,6 +27,7 @@
 // (border) rows stay in FP64.
 #include "fgpu_internal.h"
 #include "tc_common.cuh"
+#include "potf2_block.cuh"
 
 #include <cuda.h>
 #include <cuda_fp16.h>
@@ -316,7 +317,15 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 // issues the MMAs (N = 32 NQ) into TMEM (two buffers of 7 x 32 columns for
 // NQ = 1, one of 7 x 64 for NQ = 2), warps 0-3 drain the level sums in groups
 // of 8 columns and subtract the exactly converted sums from K; warp 6 applies
-// the same coupling to the right-hand-side rows in FP64.
+// the same coupling to the right-hand-side rows in FP64.  Once the epilogue
+// warps have coupled a problem's own 128-row tile, they factor quarter dq's
+// 32 x 32 diagonal block right there (barrier 1 among the four warps).
+// Tiles are handed out dynamically (an atomic counter over a host-built
+// order in which every problem's own row tile comes first), so the CTAs
+// that factor a diagonal block take correspondingly fewer tiles and the
+// factors' FP64 latency hides behind the other CTAs' couplings.  The
+// producer lane fetches each tile id and passes it to the MMA and epilogue
+// warps through a 4-entry ring in shared memory.
 // ---------------------------------------------------------------------------
 constexpr int CPL_NSTAGE = 3;
 constexpr uint32_t CPL_SMEM = CPL_NSTAGE * STAGE + 256;
@@ -325,7 +334,7 @@ constexpr int CPL_THREADS = 224;  // warps 0-3 epilogue, 4 TMA, 5 MMA, 6 right-h
 template <int NQ>
 __global__ void __launch_bounds__(CPL_THREADS, 1)
     k_couple(const Prob* __restrict__ probs, int nprob, int s, int sq, int ns, int dq,
-             const int* __restrict__ prefix) {
+             const int* __restrict__ order, int total, int* __restrict__ counter) {
   constexpr int N = 32 * NQ;
   constexpr uint32_t B_BYTES = NSLICE * 2 * N * 16;    // 7 planes x 2 k-groups x N rows x 16 B
   constexpr uint32_t CSTAGE = A_STAGE + B_BYTES;
@@ -336,8 +345,12 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
   uint64_t* empty = full + CPL_NSTAGE;
   uint64_t* tfull = full + 2 * CPL_NSTAGE;  // [2]
   uint64_t* tempty = tfull + 2;             // [2]
-  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 4);
+  uint64_t* idf = tfull + 4;                // [4] tile id published
+  uint64_t* ide = tfull + 8;                // [4] tile id read by the MMA lane and the 128 epilogue threads
+  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 12);
   __shared__ int s_abort;
+  __shared__ int s_tile[4];
+  __shared__ PotfShared<QW> s_potf;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nch = 2 * ns;
   if (tid == 0) {
@@ -350,6 +363,10 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
       mbar_init(&tfull[k], 1);
       mbar_init(&tempty[k], 128);
     }
+    for (int k = 0; k < 4; ++k) {
+      mbar_init(&idf[k], 1);
+      mbar_init(&ide[k], 129);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 5) {
@@ -360,24 +377,31 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tbase = *slot;
-  const int total = prefix[nprob];
-  auto decode = [&](int t, int& p, int& ti) {
-    int lo = 0, hi = nprob;  // largest p with prefix[p] <= t
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (prefix[mid] <= t) lo = mid; else hi = mid;
-    }
-    p = lo;
-    ti = s + (t - prefix[lo]);
+  // next tile id from the ring (-1: no more tiles); false if the wait gave up
+  auto next_tile = [&](uint32_t k, int& id) -> bool {
+    const int sl = k & 3;
+    if (!mbar_wait(&idf[sl], (k >> 2) & 1)) return false;
+    id = *(volatile int*)&s_tile[sl];
+    mbar_arrive(&ide[sl]);
+    return true;
   };
 
   if (warp == 4) {
-    // ---------------- TMA producer ----------------
+    // ---------------- TMA producer (and tile fetcher) ----------------
     if (lane == 0) {
       uint32_t g = 0;
-      for (int t = blockIdx.x; t < total && !s_abort; t += gridDim.x) {
-        int p, ti;
-        decode(t, p, ti);
+      for (uint32_t k = 0;; ++k) {
+        const int sl = k & 3;
+        if (!mbar_wait(&ide[sl], ((k >> 2) & 1) ^ 1)) {
+          s_abort = 1;
+          break;
+        }
+        const int u = s_abort ? total : atomicAdd(counter, 1);
+        const int id = u < total ? order[u] : -1;
+        s_tile[sl] = id;
+        mbar_arrive(&idf[sl]);
+        if (id < 0) break;
+        const int p = id >> 16, ti = id & 0xFFFF;
         const Prob& P = probs[p];
         const void* tb = NQ == 1 ? P.tmap_b32 : P.tmap_b;
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
@@ -402,7 +426,13 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
       uint32_t g = 0, it = 0;
       const uint64_t adesc0 = smem_desc(su32(smq), 2048, 128);
       const uint64_t bdesc0 = smem_desc(su32(smq) + A_STAGE, N * 16, 128);
-      for (int t = blockIdx.x; t < total && !s_abort; t += gridDim.x, ++it) {
+      for (uint32_t k = 0;; ++k, ++it) {
+        int id;
+        if (!next_tile(k, id)) {
+          s_abort = 1;
+          break;
+        }
+        if (id < 0) break;
         const int buf = it % NBUF;
         const uint32_t use = it / NBUF;
         if (!mbar_wait(&tempty[buf], (use & 1) ^ 1)) {
@@ -451,9 +481,14 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
   } else {
     // ---------------- epilogue (warps 0-3): row = TMEM lane ----------------
     uint32_t it = 0;
-    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
-      int p, ti;
-      decode(t, p, ti);
+    for (uint32_t k = 0;; ++k, ++it) {
+      int id;
+      if (!next_tile(k, id)) {
+        s_abort = 1;
+        break;
+      }
+      if (id < 0) break;
+      const int p = id >> 16, ti = id & 0xFFFF;
       const Prob& P = probs[p];
       const int buf = it % NBUF;
       const uint32_t use = it / NBUF;
@@ -497,6 +532,11 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       mbar_arrive(&tempty[buf]);
+      if (ti == s) {
+        // the problem's own row tile holds quarter dq's diagonal block: factor it
+        bar_sync_n(1, 128);  // every coupled entry of the tile written and visible
+        if (!*(volatile int*)&P.status[1]) potf2_block<QW>(P, cd, s * (NB / QW) + dq, tid, s_potf, 1);
+      }
     }
   }
   __syncthreads();
@@ -609,15 +649,15 @@ cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc
 }
 
 cudaError_t launch_couple(const Prob* probs, int nprob, int step, int sq, int ns, int dq, int nq,
-                          const int* prefix, int total_tiles, int num_sms, cudaStream_t s) {
+                          const int* order, int total_tiles, int* counter, int num_sms, cudaStream_t s) {
   cudaError_t e = set_attrs();
   if (e != cudaSuccess) return e;
   int grid = total_tiles < num_sms ? total_tiles : num_sms;
   if (grid < 1) grid = 1;  // the right-hand-side rows still need their coupling
   if (nq == 1)
-    k_couple<1><<<grid, CPL_THREADS, CPL_SMEM, s>>>(probs, nprob, step, sq, ns, dq, prefix);
+    k_couple<1><<<grid, CPL_THREADS, CPL_SMEM, s>>>(probs, nprob, step, sq, ns, dq, order, total_tiles, counter);
   else
-    k_couple<2><<<grid, CPL_THREADS, CPL_SMEM, s>>>(probs, nprob, step, sq, ns, dq, prefix);
+    k_couple<2><<<grid, CPL_THREADS, CPL_SMEM, s>>>(probs, nprob, step, sq, ns, dq, order, total_tiles, counter);
   return cudaGetLastError();
 }
 
