@@ -259,8 +259,11 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) {
           long long S[NSLICE];
+          // levels 0 and 1 hold at most 2 x 128 x 128^2 = 2^22 in magnitude (|d| <= 128)
+          S[0] = small_f2i(__uint_as_float(v[0][jj]));
+          S[1] = small_f2i(__uint_as_float(v[1][jj]));
 #pragma unroll
-          for (int l = 0; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
+          for (int l = 2; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
           // W = S0 2^48 + S1 2^40 + S2 2^32 + S3 2^24 + S4 2^16 + S5 2^8 + S6
           const long long low = S[4] * 65536 + S[5] * 256 + S[6];  // |low| < 2^41
           hv[gq * 8 + jj] = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);

@@ -151,6 +151,11 @@ __device__ __forceinline__ double fixed_to_double(long long hi, int lo, int e) {
                                           (mant & 0xFFFFFFFFFFFFFULL)));
 }
 
+// an integer-valued float x with |x| <= 2^22 as an int, exactly, without a
+// conversion instruction: x + 1.5 * 2^23 lies in [2^23, 2^24], where the
+// float's low mantissa bits are x + 2^22 (one FADD and one IADD)
+__device__ __forceinline__ int small_f2i(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
+
 // tile t of step s -> (problem, 128-row tile, 64-column tile); false if out of range
 __device__ __forceinline__ bool decode_tile(const Prob* __restrict__ probs, const int* __restrict__ prefix, int nprob,
                                             int s, int t, int& p, int& ti, int& tj) {
