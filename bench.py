@@ -364,7 +364,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores, model = host_info()
-        sample = args.cpu_sample or cores
+        sample = args.cpu_sample or 5 * cores  # ~10 s of CPU work on the 16-core host
         try:
             v, dt, _, _ = cpu_baseline(p, mu, sample, cores)
             cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
