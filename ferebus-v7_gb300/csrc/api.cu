@@ -145,8 +145,7 @@ struct UpdSched {
   int num_sms = 0;
   int* build_prefix_dev = nullptr;  // nprob + 1: tiles of the tensor-core build
   int build_total = 0;
-  int* row_prefix_dev = nullptr;    // per step, nprob + 1: 128-row tiles ti >= step (quarter coupling)
-  std::vector<int> row_totals;
+  std::vector<int> row_totals;      // per step: 128-row tiles ti >= step over all problems (couplings)
   int* cpl_order_dev = nullptr;     // per step: (problem << 16 | ti) of its row tiles, own row tile first
   std::vector<size_t> cpl_off;      // offset of each step's order
   int* cpl_counter_dev = nullptr;   // per step x 3 couplings: tile counters, zeroed per evaluation
@@ -334,28 +333,16 @@ int build_sched(const std::vector<int>& nt128, const std::vector<int>& tc_build,
   CK(cudaMalloc(&u.prefix_dev, sizeof(int) * h.size()));
   if (track) track->push_back(u.prefix_dev);
   CK(cudaMemcpy(u.prefix_dev, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
-  // quarter coupling: row tiles ti >= step of every problem
+  // couplings: the row tiles ti >= step of every problem, in the order the
+  // CTAs take them: every problem's own row tile (which also carries the
+  // next quarter's diagonal factor) first
   {
-    std::vector<int> r((size_t)std::max(ntmax, 1) * u.stride, 0);
-    u.row_totals.assign(std::max(ntmax, 1), 0);
-    for (int st = 0; st < ntmax; ++st) {
-      int acc = 0;
-      for (int p = 0; p < nprob; ++p) {
-        r[(size_t)st * u.stride + p] = acc;
-        acc += std::max(0, nt128[p] - st);
-      }
-      r[(size_t)st * u.stride + nprob] = acc;
-      u.row_totals[st] = acc;
-    }
-    CK(cudaMalloc(&u.row_prefix_dev, sizeof(int) * r.size()));
-    if (track) track->push_back(u.row_prefix_dev);
-    CK(cudaMemcpy(u.row_prefix_dev, r.data(), sizeof(int) * r.size(), cudaMemcpyHostToDevice));
-    // dynamic order of the couplings' tiles: every problem's own row tile
-    // (which also carries the next quarter's diagonal factor) first
     std::vector<int> ord;
     u.cpl_off.assign(std::max(ntmax, 1), 0);
+    u.row_totals.assign(std::max(ntmax, 1), 0);
     for (int st = 0; st < ntmax; ++st) {
       u.cpl_off[st] = ord.size();
+      for (int p = 0; p < nprob; ++p) u.row_totals[st] += std::max(0, nt128[p] - st);
       for (int p = 0; p < nprob; ++p)
         if (nt128[p] > st) ord.push_back((p << 16) | st);
       for (int p = 0; p < nprob; ++p)
@@ -533,7 +520,6 @@ void free_worker(Worker* w) {
   cudaFree(w->prob_d);
   cudaFree(w->sched.prefix_dev);
   cudaFree(w->sched.build_prefix_dev);
-  cudaFree(w->sched.row_prefix_dev);
   cudaFree(w->sched.cpl_order_dev);
   cudaFree(w->sched.cpl_counter_dev);
   if (w->h_stage) cudaFreeHost(w->h_stage);
