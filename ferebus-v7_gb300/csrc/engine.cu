@@ -448,85 +448,6 @@ __global__ void __launch_bounds__(256) k_trsmw(const Prob* __restrict__ probs, i
 }
 
 // ---------------------------------------------------------------------------
-// the same solve with one thread per row: row r of the panel, x (1 x W), is
-// x L11^T = b, i.e. forward substitution x_c = (b_c - sum_{k<c} x_k L_ck) / L_cc,
-// independent for every row.  The row stays in registers and L11 is read
-// from shared memory by all threads at once (broadcast): no block barrier
-// inside the solve.  128 rows per CTA.  In tensor-core mode the thread also
-// writes the 7 fp16 digit planes of its finished row segment (factor rows
-// r < Nc), which is everything the couplings and the trailing update read
-// of this quarter: their live rows and B rows all lie below the quarter's
-// diagonal block.
-// ---------------------------------------------------------------------------
-template <int W>
-__global__ void __launch_bounds__(128) k_trsm_rows(const Prob* __restrict__ probs, int col0_step, int col0_off) {
-  const Prob& P = probs[blockIdx.y];
-  const int col0 = col0_step + col0_off;
-  const int last = P.nrt ? P.nrt - 1 : P.nsteps;  // last 64-row tile
-  const int row_end = (last + 1) * TB;
-  const int rbase = col0 + W + blockIdx.x * 128;
-  if (col0 >= P.Nc || rbase >= row_end) return;
-  if (*(volatile int*)&P.status[1]) return;
-  __shared__ double L[W * W];  // L[c * W + k] = L_ck (row c, column k), lower
-  __shared__ double rd[W];
-  const size_t ld = (size_t)P.ld;
-  const double* Ld = P.K + (size_t)col0 * ld + col0;
-  for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
-    const int c = e % W, k = e / W;  // column k, row c: coalesced over c
-    L[c * W + k] = Ld[(size_t)k * ld + c];
-  }
-  __syncthreads();
-  if (threadIdx.x < W) rd[threadIdx.x] = 1.0 / L[threadIdx.x * W + threadIdx.x];
-  __syncthreads();
-  const int r = rbase + threadIdx.x;
-  if (r >= row_end) return;
-  double* row = P.K + (size_t)col0 * ld + r;
-  double x[W];
-#pragma unroll
-  for (int c = 0; c < W; ++c) x[c] = row[(size_t)c * ld];
-#pragma unroll
-  for (int c = 0; c < W; ++c) {
-    double a = x[c];
-#pragma unroll
-    for (int k = 0; k < c; ++k) a = fma(-x[k], L[c * W + k], a);
-    x[c] = a * rd[c];
-  }
-#pragma unroll
-  for (int c = 0; c < W; ++c) row[(size_t)c * ld] = x[c];
-  if (P.mode == 1 && r < P.Nc) {
-    // digit planes, layout [row tile][plane][k-group of 8][row][8 x fp16]
-    const int e = P.escale[r];
-    bool bad = false;
-    unsigned char* base = P.slices + (size_t)(r / NB) * NSLICE * SLICE_BYTES + (size_t)(r % NB) * 16;
-    const int kg0 = (col0 % NB) / 8;
-#pragma unroll
-    for (int g = 0; g < W / 8; ++g) {
-      int d[NSLICE][8];
-#pragma unroll
-      for (int kk = 0; kk < 8; ++kk) {
-        long long F = to_fixed55(x[g * 8 + kk], e, &bad);
-#pragma unroll
-        for (int p = NSLICE - 1; p >= 1; --p) {
-          const int b = (int)(signed char)(F & 0xFF);
-          d[p][kk] = b;
-          F = (F - b) >> 8;
-        }
-        d[0][kk] = (int)F;
-      }
-#pragma unroll
-      for (int p = 0; p < NSLICE; ++p) {
-        __align__(16) __half h[8];
-#pragma unroll
-        for (int kk = 0; kk < 8; ++kk) h[kk] = __int2half_rn(d[p][kk]);
-        *reinterpret_cast<uint4*>(base + (size_t)p * SLICE_BYTES + (size_t)(kg0 + g) * 2048) =
-            *reinterpret_cast<const uint4*>(h);
-      }
-    }
-    if (bad) atomicOr(&P.status[3], 1);
-  }
-}
-
-// ---------------------------------------------------------------------------
 // trailing update C(ti, tj) -= P(ti) P(tj)^T on the FP64 MMA pipe
 // (mma.sync m8n8k4 f64).  128 threads, 4 warps x (32 x 32).
 // ---------------------------------------------------------------------------
@@ -762,13 +683,6 @@ cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s)
 cudaError_t launch_potf2_quarter(const Prob* probs, int nprob, int step, int q, cudaStream_t s) {
   // log-det parts indexed by 32-column block
   k_potf2w<QW><<<nprob, QW * 4, 0, s>>>(probs, step * NB, q * QW, step * (NB / QW), q);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_trsm_quarter(const Prob* probs, int nprob, int step, int q, int max_rows, cudaStream_t s) {
-  const int rows = max_rows - (step * NB + q * QW + QW);
-  if (rows <= 0) return cudaSuccess;
-  k_trsm_rows<QW><<<dim3((rows + 127) / 128, nprob), 128, 0, s>>>(probs, step * NB, q * QW);
   return cudaGetLastError();
 }
 

@@ -116,6 +116,7 @@ cudaError_t launch_potf2(const Prob* probs, int nprob, int step, cudaStream_t s)
 // writes their fp16 digit planes
 constexpr int QW = 32;
 cudaError_t launch_potf2_quarter(const Prob* probs, int nprob, int step, int q, cudaStream_t s);
+// quarter panel solve (ozaki.cu): FP64 substitution in two 16-column halves coupled on the tensor cores
 cudaError_t launch_trsm_quarter(const Prob* probs, int nprob, int step, int q, int max_rows, cudaStream_t s);
 // max_rowtiles: 64-row tiles of the tallest problem (0 = max_nsteps + 1)
 cudaError_t launch_trsm(const Prob* probs, int nprob, int step, int max_nsteps, cudaStream_t s,

@@ -577,6 +577,212 @@ __global__ void __launch_bounds__(256) k_border_update(const Prob* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
+// quarter panel solve with a tensor-core coupling inside the quarter: row r
+// of the panel below quarter q's diagonal block solves x L_qq^T = b by
+// forward substitution in FP64, one thread per row, but in two halves of 16
+// columns: after the first half, its digit planes (the same 55-bit fixed
+// point and 7 fp16 digits as everywhere) go to shared memory together with
+// those of L_qq's lower-left 16 x 16 block, 28 tcgen05.mma (M = 128, N = 16,
+// K = 16) form the coupling sum_{k<16} x_k L_jk with the same 7 digit-product
+// levels as the trailing update (each level an exact integer in f32), and
+// each thread subtracts it, converted with one rounding, from its row before
+// solving the second half.  That halves the FP64 substitution work of the
+// quarter.  The right-hand-side rows (no digit scale) take the coupling in
+// FP64.  Each thread also writes its row's digit planes, which is everything
+// the couplings and the trailing update read of this quarter: their rows all
+// lie below the quarter's diagonal block.  128 rows per CTA; 112 TMEM columns.
+// ---------------------------------------------------------------------------
+constexpr int TQ_H = 16;                               // half a quarter
+constexpr uint32_t TQ_A_BYTES = NSLICE * 2 * 128 * 16;  // 28 KB: first-half digits of the CTA's 128 rows
+constexpr uint32_t TQ_B_BYTES = NSLICE * 2 * 16 * 16;   // 3.5 KB: digits of L_qq rows 16..31, columns 0..15
+constexpr uint32_t TQ_SMEM = TQ_A_BYTES + TQ_B_BYTES + 64;
+constexpr uint32_t IDESC_128x16 = (1u << 4) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void digits8(const double* x, int e, bool* bad, int d[NSLICE][8]) {
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk) {
+    long long F = to_fixed55(x[kk], e, bad);
+#pragma unroll
+    for (int p = NSLICE - 1; p >= 1; --p) {
+      const int b = (int)(signed char)(F & 0xFF);
+      d[p][kk] = b;
+      F = (F - b) >> 8;
+    }
+    d[0][kk] = (int)F;
+  }
+}
+__device__ __forceinline__ uint4 pack_half8(const int* d) {
+  __align__(16) __half h[8];
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk) h[kk] = __int2half_rn(d[kk]);
+  return *reinterpret_cast<const uint4*>(h);
+}
+
+__global__ void __launch_bounds__(128) k_trsm_quarter(const Prob* __restrict__ probs, int col0_step, int col0_off) {
+  const Prob& P = probs[blockIdx.y];
+  const int col0 = col0_step + col0_off;
+  const int last = P.nrt ? P.nrt - 1 : P.nsteps;  // last 64-row tile: factor rows, then the right-hand-side rows
+  const int row_end = (last + 1) * TB;
+  const int rbase = col0 + QW + blockIdx.x * 128;
+  if (P.mode != 1 || col0 >= P.Nc || rbase >= row_end) return;
+  __shared__ int s_skip;
+  if (threadIdx.x == 0) s_skip = *(volatile int*)&P.status[1];  // one read: the exit below is block-uniform
+  __syncthreads();
+  if (s_skip) return;
+  extern __shared__ __align__(1024) unsigned char smt[];
+  unsigned char* As = smt;               // [plane][k-group 2][row 128][8 x fp16]
+  unsigned char* Bs = smt + TQ_A_BYTES;  // [plane][k-group 2][row 16][8 x fp16]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smt + TQ_A_BYTES + TQ_B_BYTES);
+  __shared__ double L[QW * QW];  // L[c * QW + k] = L_ck
+  __shared__ double rd[QW];
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const size_t ld = (size_t)P.ld;
+  const double* Ld = P.K + (size_t)col0 * ld + col0;
+  for (int e = tid; e < QW * QW; e += 128) {
+    const int c = e % QW, k = e / QW;  // coalesced over c
+    L[c * QW + k] = Ld[(size_t)k * ld + c];
+  }
+  if (tid == 0) {
+    s_fail = 0;
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(su32(&s_tmem)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = s_tmem;
+  bool bad = false;
+  if (tid < QW) rd[tid] = 1.0 / L[tid * QW + tid];
+  if (tid >= 64 && tid < 96) {
+    // B: rows 16..31 of L_qq, columns 0..15 (one thread per row and k-group)
+    const int t = tid - 64, j = TQ_H + (t >> 1), g = t & 1;
+    int d[NSLICE][8];
+    digits8(&L[j * QW + g * 8], P.escale[col0 + j], &bad, d);
+#pragma unroll
+    for (int p = 0; p < NSLICE; ++p)
+      *reinterpret_cast<uint4*>(Bs + p * 512 + g * 256 + (j - TQ_H) * 16) = pack_half8(d[p]);
+  }
+  __syncthreads();
+  const int r = rbase + tid;
+  const bool live = r < row_end;
+  const bool fac = live && r < P.Nc;  // factor row: digit planes and the tensor-core coupling
+  double x[QW];
+  double* row = P.K + (size_t)col0 * ld + r;
+#pragma unroll
+  for (int c = 0; c < QW; ++c) x[c] = live ? row[(size_t)c * ld] : 0.0;
+  // first half
+#pragma unroll
+  for (int c = 0; c < TQ_H; ++c) {
+    double a = x[c];
+#pragma unroll
+    for (int k = 0; k < c; ++k) a = fma(-x[k], L[c * QW + k], a);
+    x[c] = a * rd[c];
+  }
+  const int er = fac ? P.escale[r] : 0;
+  unsigned char* gbase = P.slices + (size_t)(r / NB) * NSLICE * SLICE_BYTES + (size_t)(r % NB) * 16;
+  const int kg0 = (col0 % NB) / 8;
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    int d[NSLICE][8];
+    if (fac) {
+      digits8(&x[g * 8], er, &bad, d);
+    } else {
+#pragma unroll
+      for (int p = 0; p < NSLICE; ++p)
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) d[p][kk] = 0;
+    }
+#pragma unroll
+    for (int p = 0; p < NSLICE; ++p) {
+      const uint4 v = pack_half8(d[p]);
+      *reinterpret_cast<uint4*>(As + p * 4096 + g * 2048 + tid * 16) = v;
+      if (fac) *reinterpret_cast<uint4*>(gbase + (size_t)p * SLICE_BYTES + (size_t)(kg0 + g) * 2048) = v;
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // digits visible to the tensor cores
+  __syncthreads();
+  if (tid == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint64_t a0 = smem_desc(su32(As), 2048, 128), b0 = smem_desc(su32(Bs), 256, 128);
+#pragma unroll
+    for (int pp = 0; pp < NSLICE; ++pp)
+#pragma unroll
+      for (int q = 0; q + pp < NSLICE; ++q)
+        mma_f16_desc(tmem + (uint32_t)(pp + q) * 16, a0 + (uint64_t)((pp * 4096) >> 4), b0 + (uint64_t)((q * 512) >> 4),
+                     IDESC_128x16, pp == 0 ? 0u : 1u);
+    mma_commit(bar);
+  }
+  if (!mbar_wait(bar, 0)) s_fail = 1;
+  asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    uint32_t v[NSLICE][8];
+#pragma unroll
+    for (int l = 0; l < NSLICE; ++l)
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                   : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]), "=r"(v[l][5]),
+                     "=r"(v[l][6]), "=r"(v[l][7])
+                   : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * 16 + g * 8)));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+    if (fac) {
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) {
+        long long S[NSLICE];  // every level <= 7 x 16 x 128^2 < 2^22
+#pragma unroll
+        for (int l = 0; l < NSLICE; ++l) S[l] = small_f2i(__uint_as_float(v[l][jj]));
+        const long long low = S[4] * 65536 + S[5] * 256 + S[6];
+        const long long hi = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
+        const int j = TQ_H + g * 8 + jj;
+        x[j] -= fixed_to_double(hi, (int)(low & 0xFFFFFF), er - 62 + P.escale[col0 + j]);
+      }
+    }
+  }
+  if (live && !fac) {
+    // right-hand-side rows: the coupling in FP64
+#pragma unroll
+    for (int j = TQ_H; j < QW; ++j) {
+      double a = x[j];
+#pragma unroll
+      for (int k = 0; k < TQ_H; ++k) a = fma(-x[k], L[j * QW + k], a);
+      x[j] = a;
+    }
+  }
+  // second half
+#pragma unroll
+  for (int c = TQ_H; c < QW; ++c) {
+    double a = x[c];
+#pragma unroll
+    for (int k = TQ_H; k < c; ++k) a = fma(-x[k], L[c * QW + k], a);
+    x[c] = a * rd[c];
+  }
+  if (fac) {
+#pragma unroll
+    for (int g = 2; g < 4; ++g) {
+      int d[NSLICE][8];
+      digits8(&x[g * 8], er, &bad, d);
+#pragma unroll
+      for (int p = 0; p < NSLICE; ++p)
+        *reinterpret_cast<uint4*>(gbase + (size_t)p * SLICE_BYTES + (size_t)(kg0 + g) * 2048) = pack_half8(d[p]);
+    }
+  }
+  if (live) {
+#pragma unroll
+    for (int c = 0; c < QW; ++c) row[(size_t)c * ld] = x[c];
+  }
+  if (bad) atomicOr(&P.status[3], 1);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (tid == 0 && s_fail) atomicExch(&P.status[2], 1);
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+}
+
+// ---------------------------------------------------------------------------
 // host: TMA tensor maps over a problem's digit-plane buffer
 // buffer layout: [row tile nt128][plane 7][k-group 16][row 128][8 fp16]; a (k-group, plane)
 // block is 2 KB contiguous
@@ -648,6 +854,14 @@ cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc
   const int rows = max_nc - step * NB;
   if (step == 0 || rows <= 0) return cudaSuccess;
   k_panel_prep<<<dim3((rows + 255) / 256, NB / 16, nprob), 256, 0, s>>>(probs, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trsm_quarter(const Prob* probs, int nprob, int step, int q, int max_rows, cudaStream_t s) {
+  static_assert(TQ_SMEM + (QW * QW + QW) * sizeof(double) + 16 <= 48 * 1024, "no opt-in needed below 48 KB");
+  const int rows = max_rows - (step * NB + q * QW + QW);
+  if (rows <= 0) return cudaSuccess;
+  k_trsm_quarter<<<dim3((rows + 127) / 128, nprob), 128, TQ_SMEM, s>>>(probs, step * NB, q * QW);
   return cudaGetLastError();
 }
 
