@@ -315,14 +315,17 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 // for rows i >= c0 + 32 dq, from the digit planes of the source quarters.
 // The panel uses three: quarter 0 -> 1, half 0 -> half 1, quarter 2 -> 3.
 // Persistent and warp-specialised like the trailing update: one lane of
-// warp 4 streams the k-chunks of each 128-row tile (A: 128 rows; B: the
-// destination's 32 NQ rows) through a 3-stage ring, one lane of warp 5
+// warp 8 streams the k-chunks of each 128-row tile (A: 128 rows; B: the
+// destination's 32 NQ rows) through a 3-stage ring, one lane of warp 9
 // issues the MMAs (N = 32 NQ) into TMEM (two buffers of 7 x 32 columns for
-// NQ = 1, one of 7 x 64 for NQ = 2), warps 0-3 drain the level sums in groups
-// of 8 columns and subtract the exactly converted sums from K; warp 6 applies
-// the same coupling to the right-hand-side rows in FP64.  Once the epilogue
-// warps have coupled a problem's own 128-row tile, they factor quarter dq's
-// 32 x 32 diagonal block right there (barrier 1 among the four warps).
+// NQ = 1, one of 7 x 64 for NQ = 2), warps 0-7 drain the level sums (warps w
+// and w + 4 share TMEM lanes 32 (w % 4) and take half of the columns each,
+// in groups of 8 with the next group's K entries in flight; two warps per
+// SMSP hide the integer conversion's latency) and subtract the exactly
+// converted sums from K; warp 10 applies the same coupling to the
+// right-hand-side rows in FP64.  Once the epilogue warps have coupled a
+// problem's own 128-row tile (barrier 1), warps 0-3 factor quarter dq's
+// 32 x 32 diagonal block right there (barrier 2).
 // Tiles are handed out dynamically (an atomic counter over a host-built
 // order in which every problem's own row tile comes first), so the CTAs
 // that factor a diagonal block take correspondingly fewer tiles and the
@@ -332,7 +335,8 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 // ---------------------------------------------------------------------------
 constexpr int CPL_NSTAGE = 3;
 constexpr uint32_t CPL_SMEM = CPL_NSTAGE * STAGE + 256;
-constexpr int CPL_THREADS = 224;  // warps 0-3 epilogue, 4 TMA, 5 MMA, 6 right-hand-side rows
+constexpr int CPL_THREADS = 352;  // warps 0-7 epilogue, 8 TMA, 9 MMA, 10 right-hand-side rows
+constexpr int CPL_EPI = 256;      // epilogue threads
 
 template <int NQ>
 __global__ void __launch_bounds__(CPL_THREADS, 1)
@@ -349,7 +353,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
   uint64_t* tfull = full + 2 * CPL_NSTAGE;  // [2]
   uint64_t* tempty = tfull + 2;             // [2]
   uint64_t* idf = tfull + 4;                // [4] tile id published
-  uint64_t* ide = tfull + 8;                // [4] tile id read by the MMA lane and the 128 epilogue threads
+  uint64_t* ide = tfull + 8;                // [4] tile id read by the MMA lane and the 256 epilogue threads
   uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 12);
   __shared__ int s_abort;
   __shared__ int s_tile[4];
@@ -364,15 +368,15 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
     }
     for (int k = 0; k < 2; ++k) {
       mbar_init(&tfull[k], 1);
-      mbar_init(&tempty[k], 128);
+      mbar_init(&tempty[k], CPL_EPI);
     }
     for (int k = 0; k < 4; ++k) {
       mbar_init(&idf[k], 1);
-      mbar_init(&ide[k], 129);
+      mbar_init(&ide[k], CPL_EPI + 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 5) {
+  if (warp == 9) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -389,7 +393,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
     return true;
   };
 
-  if (warp == 4) {
+  if (warp == 8) {
     // ---------------- TMA producer (and tile fetcher) ----------------
     if (lane == 0) {
       uint32_t g = 0;
@@ -423,7 +427,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
         }
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       uint32_t g = 0, it = 0;
@@ -464,25 +468,36 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
         mma_commit(&tfull[buf]);
       }
     }
-  } else if (warp == 6) {
+  } else if (warp == 10) {
     // ---------------- right-hand-side rows (FP64), problems round-robin ----------------
     for (int p = blockIdx.x; p < nprob; p += gridDim.x) {
       const Prob& P = probs[p];
       if (P.mode != 1 || s >= P.nt128 || P.status[1]) continue;
       const size_t ld = (size_t)P.ld;
-      const int c0 = s * NB;
+      const int kb = s * NB + sq * QW;  // first source column; ns == NQ source quarters
+      const int jb = s * NB + dq * QW;  // first destination column
       for (int b = 0; b < P.nrhs; ++b) {
-        for (int jj = lane; jj < N; jj += 32) {
-          const int j = c0 + dq * QW + jj;
-          double a = 0.0;
-          for (int k = sq * QW; k < (sq + ns) * QW; ++k)
-            a = fma(P.K[(size_t)(c0 + k) * ld + P.Nc + b], P.K[(size_t)(c0 + k) * ld + j], a);
-          P.K[(size_t)j * ld + P.Nc + b] -= a;
+        const double* zrow = P.K + P.Nc + b;  // right-hand-side row b: column c at c * ld
+        double zr[NQ];                        // lane l: the row's entries at source columns l, l + 32
+#pragma unroll
+        for (int h = 0; h < NQ; ++h) zr[h] = zrow[(size_t)(kb + 32 * h + lane) * ld];
+#pragma unroll
+        for (int h = 0; h < NQ; ++h) {  // destination column jb + 32 h + lane
+          const int j = jb + 32 * h + lane;
+          double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+          for (int h2 = 0; h2 < NQ; ++h2)
+#pragma unroll 8
+            for (int k = 0; k < 32; ++k)
+              acc[k & 3] = fma(__shfl_sync(0xffffffffu, zr[h2], k), P.K[(size_t)(kb + 32 * h2 + k) * ld + j], acc[k & 3]);
+          P.K[(size_t)j * ld + P.Nc + b] -= (acc[0] + acc[1]) + (acc[2] + acc[3]);
         }
       }
     }
   } else {
-    // ---------------- epilogue (warps 0-3): row = TMEM lane ----------------
+    // ---------------- epilogue (warps 0-7): row = TMEM lane ----------------
+    constexpr int NH = N / 2;  // columns per warp
+    const int lq = warp & 3, hf = warp >> 2;
     uint32_t it = 0;
     for (uint32_t k = 0;; ++k, ++it) {
       int id;
@@ -495,50 +510,64 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
       const Prob& P = probs[p];
       const int buf = it % NBUF;
       const uint32_t use = it / NBUF;
+      const int cd = s * NB + dq * QW;
+      const int i = ti * NB + 32 * lq + lane;
+      const bool live = i >= cd && i < P.Nc;
+      const size_t ld = (size_t)P.ld;
+      double* kcol = P.K + (size_t)(cd + hf * NH) * ld + i;
+      // the first group's K entries, the row scale and this half's column
+      // scales (lane l: column hf NH + l) load while the MMAs run
+      double kv[8];
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) kv[jj] = live ? kcol[(size_t)jj * ld] : 0.0;
+      const int ei = P.escale[i < P.Nc ? i : 0] - 62;
+      const int ecol = P.escale[cd + hf * NH + (lane % NH)];
       if (!mbar_wait(&tfull[buf], use & 1)) {
         s_abort = 1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const int cd = s * NB + dq * QW;
-      const int i = ti * NB + tid;
-      const bool live = i >= cd && i < P.Nc;
-      const int ei = P.escale[i < P.Nc ? i : 0] - 62;
-      const size_t ld = (size_t)P.ld;
-      double* kcol = P.K + (size_t)cd * ld + i;
 #pragma unroll 1
-      for (int g = 0; g < N / 8; ++g) {
+      for (int g = 0; g < NH / 8; ++g) {
         uint32_t v[NSLICE][8];
 #pragma unroll
         for (int l = 0; l < NSLICE; ++l)
           asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                        : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
                          "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
-                       : "r"(tbase + (uint32_t)buf * 256 + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * N + g * 8)));
+                       : "r"(tbase + (uint32_t)buf * 256 + ((uint32_t)(lq * 32) << 16) +
+                             (uint32_t)(l * N + hf * NH + g * 8)));
+        double kn[8];  // the next group's K entries
+        const bool more = live && g + 1 < NH / 8;
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) kn[jj] = more ? kcol[(size_t)((g + 1) * 8 + jj) * ld] : 0.0;
         asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+          const int ej = __shfl_sync(0xffffffffu, ecol, g * 8 + jj);
+          long long S[NSLICE];
+#pragma unroll
+          for (int l = 0; l < NSLICE; ++l)  // level l sums (l + 1) x K products of |d| <= 128: <= 2^22 for (l + 1) K <= 256
+            S[l] = (l + 1) * 32 * NQ <= 256 ? small_f2i(__uint_as_float(v[l][jj]))
+                                             : (long long)__float2int_rn(__uint_as_float(v[l][jj]));
+          const long long low = S[4] * 65536 + S[5] * 256 + S[6];
+          const long long hi = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
+          kv[jj] -= fixed_to_double(hi, (int)(low & 0xFFFFFF), ei + ej);
+        }
         if (live) {
-          double kv[8];
-#pragma unroll
-          for (int jj = 0; jj < 8; ++jj) kv[jj] = kcol[(size_t)(g * 8 + jj) * ld];
-#pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            long long S[NSLICE];
-#pragma unroll
-            for (int l = 0; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
-            const long long low = S[4] * 65536 + S[5] * 256 + S[6];
-            const long long hi = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
-            kv[jj] -= fixed_to_double(hi, (int)(low & 0xFFFFFF), ei + P.escale[cd + g * 8 + jj]);
-          }
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) kcol[(size_t)(g * 8 + jj) * ld] = kv[jj];
         }
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) kv[jj] = kn[jj];
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       mbar_arrive(&tempty[buf]);
       if (ti == s) {
         // the problem's own row tile holds quarter dq's diagonal block: factor it
-        bar_sync_n(1, 128);  // every coupled entry of the tile written and visible
-        if (!*(volatile int*)&P.status[1]) potf2_block<QW>(P, cd, s * (NB / QW) + dq, tid, s_potf, 1);
+        bar_sync_n(1, CPL_EPI);  // every coupled entry of the tile written and visible
+        if (warp < 4 && !*(volatile int*)&P.status[1])
+          potf2_block<QW>(P, cd, s * (NB / QW) + dq, tid, s_potf, 2);
       }
     }
   }
@@ -547,7 +576,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
     for (int k = 0; k < nprob; ++k) atomicExch(&probs[k].status[2], 1);
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
-  if (warp == 5) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
+  if (warp == 9) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
 }
 
 // ---------------------------------------------------------------------------
