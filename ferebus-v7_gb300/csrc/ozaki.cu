@@ -98,7 +98,7 @@ constexpr int NSTAGE = 3;
 constexpr uint32_t ACC_HI_TILE = 128 * 64 * 8;       // accumulator tile, high words (64 KB)
 constexpr uint32_t ACC_LO_TILE = 128 * 64 * 4;       // low 24-bit words (32 KB)
 constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + ACC_HI_TILE + ACC_LO_TILE + 256;
-constexpr int UPD_THREADS = 320;
+constexpr int UPD_THREADS = 352;  // warps 0-7 epilogue, 8 TMA, 9 and 10 MMA issue
 
 __global__ void __launch_bounds__(UPD_THREADS, 1)
     k_ozaki_update(const Prob* __restrict__ probs, int nprob, int s, const int* __restrict__ prefix) {
@@ -118,9 +118,9 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
     s_abort = 0;
     for (int k = 0; k < NSTAGE; ++k) {
       mbar_init(&full[k], 1);
-      mbar_init(&empty[k], 1);
+      mbar_init(&empty[k], 2);  // a commit from each MMA warp
     }
-    mbar_init(tfull, 1);
+    mbar_init(tfull, 2);
     mbar_init(tempty, 256);
     mbar_init(afull, 1);
     mbar_init(aempty, 256);
@@ -184,8 +184,13 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
         ++it;
       }
     }
-  } else if (warp == 9) {
-    // ---------------- MMA issuer ----------------
+  } else if (warp == 9 || warp == 10) {
+    // ---------------- MMA issue: two warps, disjoint level accumulators ----------------
+    // warp 9 issues the digit pairs of levels 0-4 (15 MMAs per k-chunk), warp
+    // 10 those of levels 5-6 (13): while one waits on a barrier the other's
+    // MMAs keep the tensor pipe fed.  Each level's MMAs stay in one thread,
+    // in order, so its first (accumulate = 0) MMA precedes the others.
+    const bool low_levels = warp == 9;
     if (lane == 0) {
       uint32_t g = 0, it = 0;
       const uint64_t adesc0 = smem_desc(su32(smu), 2048, 128);
@@ -208,13 +213,22 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint64_t soff = (uint64_t)((st * STAGE) >> 4);
+          if (low_levels) {
 #pragma unroll
-          for (int pp = 0; pp < NSLICE; ++pp) {
+            for (int pp = 0; pp < NSLICE; ++pp)
 #pragma unroll
-            for (int q = 0; q + pp < NSLICE; ++q) {
-              mma_f16(tbase + (uint32_t)(pp + q) * 64, adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
-                      bdesc0 + soff + (uint64_t)(q * 2048 >> 4), (c == 0 && pp == 0) ? 0u : 1u);
-            }
+              for (int q = 0; q + pp < NSLICE; ++q)
+                if (pp + q <= 4)
+                  mma_f16(tbase + (uint32_t)(pp + q) * 64, adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
+                          bdesc0 + soff + (uint64_t)(q * 2048 >> 4), (c == 0 && pp == 0) ? 0u : 1u);
+          } else {
+#pragma unroll
+            for (int pp = 0; pp < NSLICE; ++pp)
+#pragma unroll
+              for (int q = 0; q + pp < NSLICE; ++q)
+                if (pp + q > 4)
+                  mma_f16(tbase + (uint32_t)(pp + q) * 64, adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
+                          bdesc0 + soff + (uint64_t)(q * 2048 >> 4), (c == 0 && pp == 0) ? 0u : 1u);
           }
           mma_commit(&empty[st]);
         }
@@ -647,7 +661,7 @@ __device__ __forceinline__ uint4 pack_half8(const int* d) {
   return *reinterpret_cast<const uint4*>(h);
 }
 
-__global__ void __launch_bounds__(128) k_trsm_quarter(const Prob* __restrict__ probs, int col0_step, int col0_off) {
+__global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict__ probs, int col0_step, int col0_off) {
   const Prob& P = probs[blockIdx.y];
   const int col0 = col0_step + col0_off;
   const int last = P.nrt ? P.nrt - 1 : P.nsteps;  // last 64-row tile: factor rows, then the right-hand-side rows
