@@ -164,7 +164,7 @@ struct Workspace {
   long long* acc_hi = nullptr;
   int* acc_lo = nullptr;
   unsigned char* slices = nullptr;
-  unsigned char* tmaps = nullptr;  // 3 x 128 B TMA tensor maps over slices (128-, 64-, 32-row boxes)
+  unsigned char* tmaps = nullptr;  // 4 x 128 B TMA tensor maps over slices (128-, 64-, 32-row boxes; 64 rows, planes stacked)
   double* splanes = nullptr;       // theta-scaled planes (dot-product build)
   double* norms = nullptr;
   long long* fnorm = nullptr;      // tensor-core build: W_ii of the distance leaves
@@ -301,6 +301,7 @@ void fill_prob(Prob& p, const fgpu_ctx* c, const double* theta_d, const Workspac
   p.tmap_a = ws.tmaps;
   p.tmap_b = ws.tmaps ? ws.tmaps + 128 : nullptr;
   p.tmap_b32 = ws.tmaps ? ws.tmaps + 256 : nullptr;
+  p.tmap_bs = ws.tmaps ? ws.tmaps + 384 : nullptr;
   p.splanes = ws.splanes;
   p.norms = ws.norms;
   p.plane_max = c->plane_max_d;
@@ -482,11 +483,11 @@ int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track)
     CK(cudaMalloc(&ws.fnorm, sizeof(long long) * 2 * nc));
     CK(cudaMalloc(&ws.fcoef, sizeof(double) * 4));
     CK(cudaMalloc(&ws.fscale, sizeof(int) * 2));
-    CK(cudaMalloc(&ws.tmaps, 384));
-    alignas(64) unsigned char maps[384];
+    CK(cudaMalloc(&ws.tmaps, 512));
+    alignas(64) unsigned char maps[512];
     const int er = encode_slice_maps(maps, ws.slices, c->nt128);
     if (er != 0) return fail(FGPU_ECUDA, "cuTensorMapEncodeTiled failed (%d)", er);
-    CK(cudaMemcpy(ws.tmaps, maps, 384, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ws.tmaps, maps, 512, cudaMemcpyHostToDevice));
   }
   if (track) {
     for (void* q : {(void*)ws.K, (void*)ws.logdet_part, (void*)ws.out, (void*)ws.z, (void*)ws.escale,

@@ -82,6 +82,7 @@ struct Prob {
   const void* tmap_a;             // TMA tensor map over slices, box 8 x 128 rows x 2 kgroups x 7 planes
   const void* tmap_b;             // same, box of 64 rows
   const void* tmap_b32;           // same, box of 32 rows (quarter-panel coupling)
+  const void* tmap_bs;            // box of 64 rows landing as [k-group][plane][row]: the 7 planes stacked along N
   // dot-product kernel build (mode 1): planes scaled by sqrt(l_k) per evaluation
   double* splanes;                // nplanes x Nc
   double* norms;                  // MAX_LEAF x Nc: sum_k u_ik^2 of rbf leaves
@@ -97,9 +98,9 @@ struct Prob {
   int* fscale;                    // 2: s of the distance leaves, max |f| < 2^s
 };
 
-// Encode the three 5-D TMA tensor maps of a problem's digit-plane buffer
-// (boxes of 128, 64 and 32 rows) into host memory (3 x 128 bytes).  Returns 0
-// or a CUDA driver error code.
+// Encode the four 5-D TMA tensor maps of a problem's digit-plane buffer
+// (boxes of 128, 64 and 32 rows, and 64 rows with the planes stacked) into
+// host memory (4 x 128 bytes).  Returns 0 or a CUDA driver error code.
 int encode_slice_maps(void* host_maps, const void* slices, int nt128);
 
 // Launch helpers (engine.cu).  All kernels take a device array of problems

@@ -98,7 +98,31 @@ constexpr int NSTAGE = 3;
 constexpr uint32_t ACC_HI_TILE = 128 * 64 * 8;       // accumulator tile, high words (64 KB)
 constexpr uint32_t ACC_LO_TILE = 128 * 64 * 4;       // low 24-bit words (32 KB)
 constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + ACC_HI_TILE + ACC_LO_TILE + 256;
-constexpr int UPD_THREADS = 352;  // warps 0-7 epilogue, 8 TMA, 9 and 10 MMA issue
+constexpr int UPD_MMA_WARPS = 1;
+constexpr int UPD_THREADS = 32 * (9 + UPD_MMA_WARPS);  // warps 0-7 epilogue, 8 TMA, 9 MMA issue
+
+// MMA-issuing warp of digit level l (one warp issues all levels)
+__host__ __device__ constexpr int upd_level_warp(int) { return 0; }
+
+// one k-chunk of a tile with the B planes stacked along N: for A plane pp
+// the pairs (pp, q), q = 0 .. 6 - pp, accumulate into levels pp .. 6, whose
+// TMEM blocks of 64 columns are contiguous, so they are one MMA over B
+// planes 0 .. 6 - pp (N = 64 (7 - pp), split at N = 256): 10 MMAs instead of
+// 28, and A plane pp is read from shared memory once or twice instead of
+// 7 - pp times.  N >= 128 MMAs run at the tensor pipe's full rate; N = 64
+// ones are bound by shared-memory operand bandwidth.
+__device__ __forceinline__ void upd_issue_chunk(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first) {
+#pragma unroll
+  for (int pp = 0; pp < NSLICE; ++pp) {
+#pragma unroll
+    for (int q0 = 0; q0 < NSLICE - pp; q0 += 4) {
+      const int nq = (NSLICE - pp - q0) < 4 ? (NSLICE - pp - q0) : 4;  // planes in this MMA
+      const uint32_t idesc = (1u << 4) | ((uint32_t)(64 * nq >> 3) << 17) | ((128u >> 4) << 24);
+      mma_f16_desc(tbase + (uint32_t)(pp + q0) * 64, adesc + (uint64_t)(pp * 4096 >> 4),
+                   bdesc + (uint64_t)(q0 * 1024 >> 4), idesc, (first && pp == 0) ? 0u : 1u);
+    }
+  }
+}
 
 __global__ void __launch_bounds__(UPD_THREADS, 1)
     k_ozaki_update(const Prob* __restrict__ probs, int nprob, int s, const int* __restrict__ prefix) {
@@ -108,20 +132,20 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
   uint64_t* full = reinterpret_cast<uint64_t*>(smu + NSTAGE * STAGE + ACC_HI_TILE + ACC_LO_TILE);
   uint64_t* empty = full + NSTAGE;
   uint64_t* tfull = full + 2 * NSTAGE;
-  uint64_t* tempty = tfull + 1;
-  uint64_t* afull = tfull + 2;   // accumulator tile landed in shared memory
-  uint64_t* aempty = tfull + 3;  // epilogue done with the accumulator tile
-  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 4);
+  uint64_t* tempty = tfull + 1;                     // [UPD_MMA_WARPS]: that warp's levels drained
+  uint64_t* afull = tfull + 1 + UPD_MMA_WARPS;      // accumulator tile landed in shared memory
+  uint64_t* aempty = afull + 1;                     // epilogue done with the accumulator tile
+  uint32_t* slot = reinterpret_cast<uint32_t*>(aempty + 1);
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     s_abort = 0;
     for (int k = 0; k < NSTAGE; ++k) {
       mbar_init(&full[k], 1);
-      mbar_init(&empty[k], 2);  // a commit from each MMA warp
+      mbar_init(&empty[k], UPD_MMA_WARPS);  // a commit from each MMA warp
     }
-    mbar_init(tfull, 2);
-    mbar_init(tempty, 256);
+    mbar_init(tfull, UPD_MMA_WARPS);
+    for (int k = 0; k < UPD_MMA_WARPS; ++k) mbar_init(&tempty[k], 256);
     mbar_init(afull, 1);
     mbar_init(aempty, 256);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -146,7 +170,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
         const Prob& P = probs[p];
         if (P.status[1]) continue;
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
-        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_b) : "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_bs) : "memory");
         // The accumulator tile goes into its shared buffer as soon as the
         // previous tile's epilogue has released it (polled between operand
         // chunks, so the chunk loads never wait for the epilogue); step 0
@@ -169,7 +193,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
           unsigned char* As = smu + st * STAGE;
           mbar_expect_tx(&full[st], STAGE);
           tma_load_5d(As, P.tmap_a, 0, 0, 2 * c, 0, ti, &full[st]);
-          tma_load_5d(As + A_STAGE, P.tmap_b, 0, (tj & 1) * 2, 2 * c, 0, tj >> 1, &full[st]);
+          tma_load_5d(As + A_STAGE, P.tmap_bs, 0, (tj & 1) * 2, 0, 2 * c, tj >> 1, &full[st]);
         }
         if (s_abort) break;
         if (!acc_issued) {
@@ -184,22 +208,18 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
         ++it;
       }
     }
-  } else if (warp == 9 || warp == 10) {
-    // ---------------- MMA issue: two warps, disjoint level accumulators ----------------
-    // warp 9 issues the digit pairs of levels 0-4 (15 MMAs per k-chunk), warp
-    // 10 those of levels 5-6 (13): while one waits on a barrier the other's
-    // MMAs keep the tensor pipe fed.  Each level's MMAs stay in one thread,
-    // in order, so its first (accumulate = 0) MMA precedes the others.
-    const bool low_levels = warp == 9;
+  } else if (warp >= 9) {
+    // ---------------- MMA issue ----------------
+    const int mw = warp - 9;
     if (lane == 0) {
       uint32_t g = 0, it = 0;
       const uint64_t adesc0 = smem_desc(su32(smu), 2048, 128);
-      const uint64_t bdesc0 = smem_desc(su32(smu) + A_STAGE, 1024, 128);
+      const uint64_t bdesc0 = smem_desc(su32(smu) + A_STAGE, NSLICE * 1024, 128);  // [k-group][plane][row]
       for (int t = blockIdx.x; t < total; t += gridDim.x) {
         int p, ti, tj;
         decode_tile(probs, prefix, nprob, s, t, p, ti, tj);
         if (probs[p].status[1]) continue;
-        if (!mbar_wait(tempty, (it & 1) ^ 1)) {
+        if (!mbar_wait(&tempty[mw], (it & 1) ^ 1)) {  // this warp's levels of the previous tile drained
           s_abort = 1;
           break;
         }
@@ -213,23 +233,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint64_t soff = (uint64_t)((st * STAGE) >> 4);
-          if (low_levels) {
-#pragma unroll
-            for (int pp = 0; pp < NSLICE; ++pp)
-#pragma unroll
-              for (int q = 0; q + pp < NSLICE; ++q)
-                if (pp + q <= 4)
-                  mma_f16(tbase + (uint32_t)(pp + q) * 64, adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
-                          bdesc0 + soff + (uint64_t)(q * 2048 >> 4), (c == 0 && pp == 0) ? 0u : 1u);
-          } else {
-#pragma unroll
-            for (int pp = 0; pp < NSLICE; ++pp)
-#pragma unroll
-              for (int q = 0; q + pp < NSLICE; ++q)
-                if (pp + q > 4)
-                  mma_f16(tbase + (uint32_t)(pp + q) * 64, adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
-                          bdesc0 + soff + (uint64_t)(q * 2048 >> 4), (c == 0 && pp == 0) ? 0u : 1u);
-          }
+          upd_issue_chunk(tbase, adesc0 + soff, bdesc0 + soff, c == 0);
           mma_commit(&empty[st]);
         }
         if (!ok) {
@@ -256,37 +260,57 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
+      // drain the level sums one MMA warp's levels at a time, releasing
+      // them at once so that its MMAs for the next tile start while the
+      // other levels drain; W = sum_l S_l 2^(8 (6 - l)) is gathered as
+      // hi 2^24 + lo on the way (lo < 3 2^24 until normalised)
       long long hv[32];
       int lv[32];
 #pragma unroll
-      for (int gq = 0; gq < 4; ++gq) {
-        const int col0 = h * 32 + gq * 8;
-        uint32_t v[NSLICE][8];
-#pragma unroll
-        for (int l = 0; l < NSLICE; ++l) {
-          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                       : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
-                         "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
-                       : "r"(tbase + lane_base + (uint32_t)(l * 64 + col0)));
-        }
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          long long S[NSLICE];
-          // levels 0 and 1 hold at most 2 x 128 x 128^2 = 2^22 in magnitude (|d| <= 128)
-          S[0] = small_f2i(__uint_as_float(v[0][jj]));
-          S[1] = small_f2i(__uint_as_float(v[1][jj]));
-#pragma unroll
-          for (int l = 2; l < NSLICE; ++l) S[l] = (long long)__float2int_rn(__uint_as_float(v[l][jj]));
-          // W = S0 2^48 + S1 2^40 + S2 2^32 + S3 2^24 + S4 2^16 + S5 2^8 + S6
-          const long long low = S[4] * 65536 + S[5] * 256 + S[6];  // |low| < 2^41
-          hv[gq * 8 + jj] = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
-          lv[gq * 8 + jj] = (int)(low & 0xFFFFFF);
-        }
+      for (int q = 0; q < 32; ++q) {
+        hv[q] = 0;
+        lv[q] = 0;
       }
-      // TMEM drained: let the next tile's MMAs start
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      mbar_arrive(tempty);
+#pragma unroll
+      for (int G = 0; G < UPD_MMA_WARPS; ++G) {
+#pragma unroll
+        for (int gq = 0; gq < 4; ++gq) {
+          const int col0 = h * 32 + gq * 8;
+          uint32_t v[NSLICE][8];
+#pragma unroll
+          for (int l = 0; l < NSLICE; ++l)
+            if (upd_level_warp(l) == G)
+              asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                           : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
+                             "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
+                           : "r"(tbase + lane_base + (uint32_t)(l * 64 + col0)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+          for (int l = 0; l < NSLICE; ++l) {
+            if (upd_level_warp(l) != G) continue;
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+              // levels 0 and 1 hold at most 2 x 128 x 128^2 = 2^22 in magnitude (|d| <= 128)
+              const int S = l <= 1 ? small_f2i(__uint_as_float(v[l][jj])) : __float2int_rn(__uint_as_float(v[l][jj]));
+              long long& hq = hv[gq * 8 + jj];
+              int& lq = lv[gq * 8 + jj];
+              if (l <= 3) {
+                hq += (long long)S << (8 * (3 - l));
+              } else {  // split at 2^24: S 2^(8 (6 - l)) = (S >> 8 (l - 3)) 2^24 + (S mod 2^(8 (l - 3))) 2^(8 (6 - l))
+                hq += S >> (8 * (l - 3));
+                lq += (S & ((1 << (8 * (l - 3))) - 1)) << (8 * (6 - l));
+              }
+            }
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        mbar_arrive(&tempty[G]);  // these TMEM columns are free for the next tile
+      }
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        hv[q] += lv[q] >> 24;
+        lv[q] &= 0xFFFFFF;
+      }
       const size_t tile = (size_t)(tj * P.nt128 + ti) * (128 * 64);
       long long* gh = P.acc_hi + tile;
       int* gl = P.acc_lo + tile;
@@ -863,6 +887,16 @@ int encode_slice_maps(void* host_maps, const void* slices, int nt128) {
          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return (int)r;
   r = fn(&m[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dims, strides, boxQ, es,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return (int)r;
+  // the same 64-row box with the plane and k-group dimensions swapped: it
+  // lands as [k-group][plane][row], so the 7 planes of a k-group are one
+  // operand of 7 x 64 rows (the trailing update's stacked-N MMAs)
+  const cuuint64_t dimsS[5] = {256, 4, (cuuint64_t)NSLICE, 16, (cuuint64_t)nt128};
+  const cuuint64_t stridesS[4] = {512, (cuuint64_t)SLICE_BYTES, 2048, (cuuint64_t)NSLICE * SLICE_BYTES};
+  const cuuint32_t boxS[5] = {256, 2, NSLICE, 2, 1};
+  r = fn(&m[3], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dimsS, stridesS, boxS, es,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return (int)r;
