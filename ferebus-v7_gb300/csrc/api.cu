@@ -164,7 +164,7 @@ struct Workspace {
   long long* acc_hi = nullptr;
   int* acc_lo = nullptr;
   unsigned char* slices = nullptr;
-  unsigned char* tmaps = nullptr;  // 4 x 128 B TMA tensor maps over slices (128-, 64-, 32-row boxes; 64 rows, planes stacked)
+  unsigned char* tmaps = nullptr;  // 4 x 128 B TMA tensor maps over slices (128-, 64-row boxes; 64, 32 rows, planes stacked)
   double* splanes = nullptr;       // theta-scaled planes (dot-product build)
   double* norms = nullptr;
   long long* fnorm = nullptr;      // tensor-core build: W_ii of the distance leaves
@@ -300,8 +300,8 @@ void fill_prob(Prob& p, const fgpu_ctx* c, const double* theta_d, const Workspac
   p.slices = ws.slices;
   p.tmap_a = ws.tmaps;
   p.tmap_b = ws.tmaps ? ws.tmaps + 128 : nullptr;
-  p.tmap_b32 = ws.tmaps ? ws.tmaps + 256 : nullptr;
-  p.tmap_bs = ws.tmaps ? ws.tmaps + 384 : nullptr;
+  p.tmap_bs = ws.tmaps ? ws.tmaps + 256 : nullptr;
+  p.tmap_bs32 = ws.tmaps ? ws.tmaps + 384 : nullptr;
   p.splanes = ws.splanes;
   p.norms = ws.norms;
   p.plane_max = c->plane_max_d;

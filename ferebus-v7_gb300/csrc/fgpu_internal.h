@@ -81,8 +81,8 @@ struct Prob {
   unsigned char* slices;          // nt128 x 7 x 32 KB: fp16 digit planes of the current panel
   const void* tmap_a;             // TMA tensor map over slices, box 8 x 128 rows x 2 kgroups x 7 planes
   const void* tmap_b;             // same, box of 64 rows
-  const void* tmap_b32;           // same, box of 32 rows (quarter-panel coupling)
   const void* tmap_bs;            // box of 64 rows landing as [k-group][plane][row]: the 7 planes stacked along N
+  const void* tmap_bs32;          // same, box of 32 rows
   // dot-product kernel build (mode 1): planes scaled by sqrt(l_k) per evaluation
   double* splanes;                // nplanes x Nc
   double* norms;                  // MAX_LEAF x Nc: sum_k u_ik^2 of rbf leaves
@@ -99,8 +99,8 @@ struct Prob {
 };
 
 // Encode the four 5-D TMA tensor maps of a problem's digit-plane buffer
-// (boxes of 128, 64 and 32 rows, and 64 rows with the planes stacked) into
-// host memory (4 x 128 bytes).  Returns 0 or a CUDA driver error code.
+// (boxes of 128 and 64 rows, and 64 and 32 rows with the planes stacked)
+// into host memory (4 x 128 bytes).  Returns 0 or a CUDA driver error code.
 int encode_slice_maps(void* host_maps, const void* slices, int nt128);
 
 // Launch helpers (engine.cu).  All kernels take a device array of problems

@@ -384,7 +384,6 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
   constexpr uint32_t B_BYTES = NSLICE * 2 * N * 16;    // 7 planes x 2 k-groups x N rows x 16 B
   constexpr uint32_t CSTAGE = A_STAGE + B_BYTES;
   constexpr int NBUF = NQ == 1 ? 2 : 1;                 // TMEM buffers of 7 N columns
-  constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((128u >> 4) << 24);
   extern __shared__ __align__(1024) unsigned char smq[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smq + CPL_NSTAGE * STAGE);
   uint64_t* empty = full + CPL_NSTAGE;
@@ -448,7 +447,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
         if (id < 0) break;
         const int p = id >> 16, ti = id & 0xFFFF;
         const Prob& P = probs[p];
-        const void* tb = NQ == 1 ? P.tmap_b32 : P.tmap_b;
+        const void* tb = NQ == 1 ? P.tmap_bs32 : P.tmap_bs;  // planes stacked along N
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tb) : "memory");
         for (int c = 0; c < nch; ++c, ++g) {
@@ -461,7 +460,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
           const int kg = 2 * (2 * sq + c);
           mbar_expect_tx(&full[st], CSTAGE);
           tma_load_5d(As, P.tmap_a, 0, 0, kg, 0, ti, &full[st]);
-          tma_load_5d(As + A_STAGE, tb, 0, dq, kg, 0, s, &full[st]);  // rows c0+32dq .. +N-1
+          tma_load_5d(As + A_STAGE, tb, 0, dq, 0, kg, s, &full[st]);  // rows c0+32dq .. +N-1
         }
       }
     }
@@ -470,7 +469,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
     if (lane == 0) {
       uint32_t g = 0, it = 0;
       const uint64_t adesc0 = smem_desc(su32(smq), 2048, 128);
-      const uint64_t bdesc0 = smem_desc(su32(smq) + A_STAGE, N * 16, 128);
+      const uint64_t bdesc0 = smem_desc(su32(smq) + A_STAGE, NSLICE * N * 16, 128);  // [k-group][plane][row]
       for (uint32_t k = 0;; ++k, ++it) {
         int id;
         if (!next_tile(k, id)) {
@@ -494,12 +493,19 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint64_t soff = (uint64_t)((st * STAGE) >> 4);
+          // A plane pp against B planes q0 .. stacked along N (at most 256
+          // rows per MMA): levels pp + q0 .. in one instruction
+          constexpr int PL = 256 / N;
 #pragma unroll
           for (int pp = 0; pp < NSLICE; ++pp)
 #pragma unroll
-            for (int qq = 0; qq + pp < NSLICE; ++qq)
-              mma_f16_desc(dt + (uint32_t)((pp + qq) * N), adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
-                           bdesc0 + soff + (uint64_t)((qq * 2 * N * 16) >> 4), IDESC, (c == 0 && pp == 0) ? 0u : 1u);
+            for (int q0 = 0; q0 < NSLICE - pp; q0 += PL) {
+              const int nq = NSLICE - pp - q0 < PL ? NSLICE - pp - q0 : PL;
+              mma_f16_desc(dt + (uint32_t)((pp + q0) * N), adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
+                           bdesc0 + soff + (uint64_t)((q0 * N * 16) >> 4),
+                           (1u << 4) | ((uint32_t)(N * nq >> 3) << 17) | ((128u >> 4) << 24),
+                           (c == 0 && pp == 0) ? 0u : 1u);
+            }
           mma_commit(&empty[st]);
         }
         if (s_abort) break;
@@ -644,26 +650,26 @@ __global__ void __launch_bounds__(256) k_border_update(const Prob* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// quarter panel solve with a tensor-core coupling inside the quarter: row r
-// of the panel below quarter q's diagonal block solves x L_qq^T = b by
-// forward substitution in FP64, one thread per row, but in two halves of 16
-// columns: after the first half, its digit planes (the same 55-bit fixed
-// point and 7 fp16 digits as everywhere) go to shared memory together with
-// those of L_qq's lower-left 16 x 16 block, 28 tcgen05.mma (M = 128, N = 16,
-// K = 16) form the coupling sum_{k<16} x_k L_jk with the same 7 digit-product
-// levels as the trailing update (each level an exact integer in f32), and
-// each thread subtracts it, converted with one rounding, from its row before
-// solving the second half.  That halves the FP64 substitution work of the
-// quarter.  The right-hand-side rows (no digit scale) take the coupling in
-// FP64.  Each thread also writes its row's digit planes, which is everything
-// the couplings and the trailing update read of this quarter: their rows all
-// lie below the quarter's diagonal block.  128 rows per CTA; 112 TMEM columns.
+// quarter panel solve with a tensor-core coupling inside the quarter: row r of
+// the panel below quarter q's diagonal block solves x L_qq^T = b by forward
+// substitution in FP64, one thread per row, but in two halves of 16 columns:
+// after the first half, its digit planes (the same 55-bit fixed point and 7
+// fp16 digits as everywhere) go to shared memory together with those of L_qq's
+// lower-left 16 x 16 block, 7 tcgen05.mma (M = 128, K = 16; B's planes stacked
+// along N, N = 16 (7 - p) for A plane p) form the coupling sum_{k<16} x_k L_jk
+// with the same 7 digit-product levels as the trailing update (each level an
+// exact integer in f32), and each thread subtracts it, converted with one
+// rounding, from its row before solving the second half.  That halves the FP64
+// substitution work of the quarter.  The right-hand-side rows (no digit scale)
+// take the coupling in FP64.  Each thread also writes its row's digit planes,
+// which is everything the couplings and the trailing update read of this
+// quarter: their rows all lie below the quarter's diagonal block.  128 rows
+// per CTA; 112 TMEM columns.
 // ---------------------------------------------------------------------------
 constexpr int TQ_H = 16;                               // half a quarter
 constexpr uint32_t TQ_A_BYTES = NSLICE * 2 * 128 * 16;  // 28 KB: first-half digits of the CTA's 128 rows
 constexpr uint32_t TQ_B_BYTES = NSLICE * 2 * 16 * 16;   // 3.5 KB: digits of L_qq rows 16..31, columns 0..15
 constexpr uint32_t TQ_SMEM = TQ_A_BYTES + TQ_B_BYTES + 64;
-constexpr uint32_t IDESC_128x16 = (1u << 4) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
 
 __device__ __forceinline__ void digits8(const double* x, int e, bool* bad, int d[NSLICE][8]) {
 #pragma unroll
@@ -698,7 +704,7 @@ __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict_
   if (s_skip) return;
   extern __shared__ __align__(1024) unsigned char smt[];
   unsigned char* As = smt;               // [plane][k-group 2][row 128][8 x fp16]
-  unsigned char* Bs = smt + TQ_A_BYTES;  // [plane][k-group 2][row 16][8 x fp16]
+  unsigned char* Bs = smt + TQ_A_BYTES;  // [k-group 2][plane][row 16][8 x fp16]: planes stacked along N
   uint64_t* bar = reinterpret_cast<uint64_t*>(smt + TQ_A_BYTES + TQ_B_BYTES);
   __shared__ double L[QW * QW];  // L[c * QW + k] = L_ck
   __shared__ double rd[QW];
@@ -733,7 +739,7 @@ __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict_
     digits8(&L[j * QW + g * 8], P.escale[col0 + j], &bad, d);
 #pragma unroll
     for (int p = 0; p < NSLICE; ++p)
-      *reinterpret_cast<uint4*>(Bs + p * 512 + g * 256 + (j - TQ_H) * 16) = pack_half8(d[p]);
+      *reinterpret_cast<uint4*>(Bs + g * (NSLICE * 256) + p * 256 + (j - TQ_H) * 16) = pack_half8(d[p]);
   }
   __syncthreads();
   const int r = rbase + tid;
@@ -776,13 +782,12 @@ __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict_
   __syncthreads();
   if (tid == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint64_t a0 = smem_desc(su32(As), 2048, 128), b0 = smem_desc(su32(Bs), 256, 128);
+    const uint64_t a0 = smem_desc(su32(As), 2048, 128), b0 = smem_desc(su32(Bs), NSLICE * 256, 128);
+    // A plane pp against B planes 0 .. 6 - pp stacked along N: levels pp .. 6
 #pragma unroll
     for (int pp = 0; pp < NSLICE; ++pp)
-#pragma unroll
-      for (int q = 0; q + pp < NSLICE; ++q)
-        mma_f16_desc(tmem + (uint32_t)(pp + q) * 16, a0 + (uint64_t)((pp * 4096) >> 4), b0 + (uint64_t)((q * 512) >> 4),
-                     IDESC_128x16, pp == 0 ? 0u : 1u);
+      mma_f16_desc(tmem + (uint32_t)pp * 16, a0 + (uint64_t)((pp * 4096) >> 4), b0,
+                   (1u << 4) | ((uint32_t)(16 * (NSLICE - pp) >> 3) << 17) | ((128u >> 4) << 24), pp == 0 ? 0u : 1u);
     mma_commit(bar);
   }
   if (!mbar_wait(bar, 0)) s_fail = 1;
@@ -875,7 +880,6 @@ int encode_slice_maps(void* host_maps, const void* slices, int nt128) {
   const cuuint64_t strides[4] = {512, 2048, (cuuint64_t)SLICE_BYTES, (cuuint64_t)NSLICE * SLICE_BYTES};
   const cuuint32_t boxA[5] = {256, 4, 2, NSLICE, 1};   // 128 rows
   const cuuint32_t boxB[5] = {256, 2, 2, NSLICE, 1};   // 64 rows
-  const cuuint32_t boxQ[5] = {256, 1, 2, NSLICE, 1};   // 32 rows
   const cuuint32_t es[5] = {1, 1, 1, 1, 1};
   CUtensorMap* m = static_cast<CUtensorMap*>(host_maps);
   CUresult r = fn(&m[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dims, strides, boxA, es,
@@ -886,17 +890,19 @@ int encode_slice_maps(void* host_maps, const void* slices, int nt128) {
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return (int)r;
-  r = fn(&m[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dims, strides, boxQ, es,
-         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return (int)r;
-  // the same 64-row box with the plane and k-group dimensions swapped: it
-  // lands as [k-group][plane][row], so the 7 planes of a k-group are one
-  // operand of 7 x 64 rows (the trailing update's stacked-N MMAs)
+  // boxes of 64 and 32 rows with the plane and k-group dimensions swapped:
+  // they land as [k-group][plane][row], so the 7 planes of a k-group are one
+  // operand of 7 x 64 (7 x 32) rows (the stacked-N MMAs of the trailing
+  // update and the couplings)
   const cuuint64_t dimsS[5] = {256, 4, (cuuint64_t)NSLICE, 16, (cuuint64_t)nt128};
   const cuuint64_t stridesS[4] = {512, (cuuint64_t)SLICE_BYTES, 2048, (cuuint64_t)NSLICE * SLICE_BYTES};
   const cuuint32_t boxS[5] = {256, 2, NSLICE, 2, 1};
-  r = fn(&m[3], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dimsS, stridesS, boxS, es,
+  const cuuint32_t boxS32[5] = {256, 1, NSLICE, 2, 1};
+  r = fn(&m[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dimsS, stridesS, boxS, es,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return (int)r;
+  r = fn(&m[3], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(slices), dimsS, stridesS, boxS32, es,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return (int)r;
