@@ -150,7 +150,20 @@ struct UpdSched {
   std::vector<size_t> cpl_off;      // offset of each step's order
   int* cpl_counter_dev = nullptr;   // per step x 3 couplings: tile counters, zeroed per evaluation
   int ncounters = 0;
+  // a second captured branch: the right-hand-side rows' trailing update runs
+  // beside the next step's panel conversion and quarter-0 factor, joined
+  // before that step's panel solve
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
+
+void free_sched_sync(UpdSched& u) {
+  if (u.fork) cudaEventDestroy(u.fork);
+  if (u.join) cudaEventDestroy(u.join);
+  if (u.side) cudaStreamDestroy(u.side);
+  u.fork = u.join = nullptr;
+  u.side = nullptr;
+}
 
 struct Workspace {
   double* K = nullptr;
@@ -331,6 +344,9 @@ int build_sched(const std::vector<int>& nt128, const std::vector<int>& tc_build,
   int dev = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&u.num_sms, cudaDevAttrMultiProcessorCount, dev));
+  CK(cudaStreamCreateWithFlags(&u.side, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&u.fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&u.join, cudaEventDisableTiming));
   CK(cudaMalloc(&u.prefix_dev, sizeof(int) * h.size()));
   if (track) track->push_back(u.prefix_dev);
   CK(cudaMemcpy(u.prefix_dev, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
@@ -407,6 +423,7 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
       STAGE(0, launch_build_tc(probs_d, nprob, us->build_prefix_dev, us->build_total, us->num_sms, s));
     STAGE(0, launch_scales(probs_d, nprob, max_nc, s));
     const int max_rows = max_nc + TB;  // the tallest problem's ld: factor rows + right-hand sides
+    bool joins = false;                // a side branch awaits its join
     for (int step = 0; step < nt; ++step) {
       if (step > 0) STAGE(5, launch_panel_prep(probs_d, nprob, step, max_nc, s));
       // four 32-column quarters: FP64 diagonal factor, panel solve (which
@@ -417,6 +434,10 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
       const int rows_total = us->row_totals[step];
       int* ctr = us->cpl_counter_dev + 3 * step;
       for (int q = 0; q < NB / QW; ++q) {
+        if (q == 0 && joins) {  // the previous step's right-hand-side rows, before they are solved
+          CK(cudaStreamWaitEvent(s, us->join, 0));
+          joins = false;
+        }
         if (q == 1) STAGE(8, launch_couple(probs_d, nprob, step, 0, 1, 1, 1, order, rows_total, ctr, us->num_sms, s));
         if (q == 2) STAGE(8, launch_couple(probs_d, nprob, step, 0, 2, 2, 2, order, rows_total, ctr + 1, us->num_sms, s));
         if (q == 3) STAGE(8, launch_couple(probs_d, nprob, step, 2, 1, 3, 1, order, rows_total, ctr + 2, us->num_sms, s));
@@ -426,9 +447,21 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
       if (step + 1 < nt) {
         STAGE(3, launch_ozaki_update(probs_d, nprob, step, nt, us->prefix_dev + (size_t)step * us->stride,
                                      us->totals[step], us->num_sms, s));
-        STAGE(7, launch_border_update(probs_d, nprob, step, max_nc, s));
+        // fork: the right-hand-side rows' FP64 update on the side branch,
+        // beside the next step's panel conversion and quarter-0 factor
+        CK(cudaEventRecord(us->fork, s));
+        CK(cudaStreamWaitEvent(us->side, us->fork, 0));
+        int r_ = mark(pe, 7, us->side, true);
+        if (r_) return r_;
+        CK(launch_border_update(probs_d, nprob, step, max_nc, us->side));
+        r_ = mark(pe, 7, us->side, false);
+        if (r_) return r_;
+        ++n;
+        CK(cudaEventRecord(us->join, us->side));
+        joins = true;
       }
     }
+    if (joins) CK(cudaStreamWaitEvent(s, us->join, 0));
     STAGE(4, launch_finalize(probs_d, nprob, s));
     if (kernels) *kernels = n;
     return 0;
@@ -523,6 +556,7 @@ void free_worker(Worker* w) {
   cudaFree(w->sched.build_prefix_dev);
   cudaFree(w->sched.cpl_order_dev);
   cudaFree(w->sched.cpl_counter_dev);
+  free_sched_sync(w->sched);
   if (w->h_stage) cudaFreeHost(w->h_stage);
   if (w->stream) cudaStreamDestroy(w->stream);
   delete w;
@@ -970,6 +1004,7 @@ void fgpu_plan_destroy(fgpu_plan* p) {
     delete p->prof;
   }
   for (void* q : p->allocations) cudaFree(q);
+  free_sched_sync(p->sched);
   if (p->h_theta) cudaFreeHost(p->h_theta);
   if (p->h_ll) cudaFreeHost(p->h_ll);
   if (p->h_info) cudaFreeHost(p->h_info);
