@@ -434,14 +434,14 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
       const int rows_total = us->row_totals[step];
       int* ctr = us->cpl_counter_dev + 3 * step;
       for (int q = 0; q < NB / QW; ++q) {
-        if (q == 0 && joins) {  // the previous step's right-hand-side rows, before they are solved
-          CK(cudaStreamWaitEvent(s, us->join, 0));
-          joins = false;
-        }
         if (q == 1) STAGE(8, launch_couple(probs_d, nprob, step, 0, 1, 1, 1, order, rows_total, ctr, us->num_sms, s));
         if (q == 2) STAGE(8, launch_couple(probs_d, nprob, step, 0, 2, 2, 2, order, rows_total, ctr + 1, us->num_sms, s));
         if (q == 3) STAGE(8, launch_couple(probs_d, nprob, step, 2, 1, 3, 1, order, rows_total, ctr + 2, us->num_sms, s));
         if (q == 0) STAGE(1, launch_potf2_quarter(probs_d, nprob, step, q, s));  // q > 0: inside the coupling
+        if (q == 0 && joins) {  // the previous step's right-hand-side rows, before they are solved
+          CK(cudaStreamWaitEvent(s, us->join, 0));
+          joins = false;
+        }
         STAGE(2, launch_trsm_quarter(probs_d, nprob, step, q, max_rows, s));  // also its digit planes
       }
       if (step + 1 < nt) {
