@@ -671,24 +671,45 @@ constexpr uint32_t TQ_A_BYTES = NSLICE * 2 * 128 * 16;  // 28 KB: first-half dig
 constexpr uint32_t TQ_B_BYTES = NSLICE * 2 * 16 * 16;   // 3.5 KB: digits of L_qq rows 16..31, columns 0..15
 constexpr uint32_t TQ_SMEM = TQ_A_BYTES + TQ_B_BYTES + 64;
 
-__device__ __forceinline__ void digits8(const double* x, int e, bool* bad, int d[NSLICE][8]) {
+// The 7 fp16 digit planes of 8 entries (one k-group of a row), packed: the
+// 55-bit fixed point F of an entry in its row scale has the balanced digits
+// d_p in [-128, 127] (p = 1..6, base 256, lowest last) and d_0 = the rest.
+// G = F + sum_{k<6} 128 256^k turns them into plain bytes: byte 6 - p of G
+// is d_p + 128, and G >> 48 is d_0 (|d_0| <= 128 when |x| <= 2^e).  A byte
+// u under the fp16 exponent bits 0x64 is the half 1024 + u, so one HSUB2 of
+// 1152 per pair of entries yields the digits exactly, with no conversion
+// instruction.  A top digit outside [-128, 128] breaks the row's scale
+// bound and sets *bad.
+__device__ __forceinline__ void digits8_packed(const double* x, int e, bool* bad, uint4 out[NSLICE]) {
+  unsigned lo[8], hi[8];
 #pragma unroll
   for (int kk = 0; kk < 8; ++kk) {
-    long long F = to_fixed55(x[kk], e, bad);
-#pragma unroll
-    for (int p = NSLICE - 1; p >= 1; --p) {
-      const int b = (int)(signed char)(F & 0xFF);
-      d[p][kk] = b;
-      F = (F - b) >> 8;
-    }
-    d[0][kk] = (int)F;
+    const long long G = to_fixed55(x[kk], e, bad) + 0x808080808080LL;
+    lo[kk] = (unsigned)G;
+    hi[kk] = (unsigned)(G >> 32);
+    if ((unsigned)(((int)hi[kk] >> 16) + 128) > 256u) *bad = true;
   }
-}
-__device__ __forceinline__ uint4 pack_half8(const int* d) {
-  __align__(16) __half h[8];
+  const __half2 off = __halves2half2(__ushort_as_half(0x6480), __ushort_as_half(0x6480));  // 1152
 #pragma unroll
-  for (int kk = 0; kk < 8; ++kk) h[kk] = __int2half_rn(d[kk]);
-  return *reinterpret_cast<const uint4*>(h);
+  for (int p = 0; p < NSLICE; ++p) {
+    unsigned w[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      unsigned u0, u1;
+      if (p == 0) {
+        u0 = (unsigned)(((int)hi[2 * m] >> 16) + 128);
+        u1 = (unsigned)(((int)hi[2 * m + 1] >> 16) + 128);
+      } else {
+        const int q = 6 - p;  // byte of G
+        u0 = (q < 4 ? lo[2 * m] >> (8 * q) : hi[2 * m] >> (8 * (q - 4))) & 0xFFu;
+        u1 = (q < 4 ? lo[2 * m + 1] >> (8 * q) : hi[2 * m + 1] >> (8 * (q - 4))) & 0xFFu;
+      }
+      const unsigned bits = (0x6400u + u0) | ((0x6400u + u1) << 16);
+      const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&bits), off);
+      w[m] = *reinterpret_cast<const unsigned*>(&h);
+    }
+    out[p] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
 }
 
 __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict__ probs, int col0_step, int col0_off) {
@@ -735,11 +756,11 @@ __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict_
   if (tid >= 64 && tid < 96) {
     // B: rows 16..31 of L_qq, columns 0..15 (one thread per row and k-group)
     const int t = tid - 64, j = TQ_H + (t >> 1), g = t & 1;
-    int d[NSLICE][8];
-    digits8(&L[j * QW + g * 8], P.escale[col0 + j], &bad, d);
+    uint4 d[NSLICE];
+    digits8_packed(&L[j * QW + g * 8], P.escale[col0 + j], &bad, d);
 #pragma unroll
     for (int p = 0; p < NSLICE; ++p)
-      *reinterpret_cast<uint4*>(Bs + g * (NSLICE * 256) + p * 256 + (j - TQ_H) * 16) = pack_half8(d[p]);
+      *reinterpret_cast<uint4*>(Bs + g * (NSLICE * 256) + p * 256 + (j - TQ_H) * 16) = d[p];
   }
   __syncthreads();
   const int r = rbase + tid;
@@ -762,18 +783,16 @@ __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict_
   const int kg0 = (col0 % NB) / 8;
 #pragma unroll
   for (int g = 0; g < 2; ++g) {
-    int d[NSLICE][8];
+    uint4 d[NSLICE];
     if (fac) {
-      digits8(&x[g * 8], er, &bad, d);
+      digits8_packed(&x[g * 8], er, &bad, d);
     } else {
 #pragma unroll
-      for (int p = 0; p < NSLICE; ++p)
-#pragma unroll
-        for (int kk = 0; kk < 8; ++kk) d[p][kk] = 0;
+      for (int p = 0; p < NSLICE; ++p) d[p] = make_uint4(0, 0, 0, 0);
     }
 #pragma unroll
     for (int p = 0; p < NSLICE; ++p) {
-      const uint4 v = pack_half8(d[p]);
+      const uint4 v = d[p];
       *reinterpret_cast<uint4*>(As + p * 4096 + g * 2048 + tid * 16) = v;
       if (fac) *reinterpret_cast<uint4*>(gbase + (size_t)p * SLICE_BYTES + (size_t)(kg0 + g) * 2048) = v;
     }
@@ -836,11 +855,11 @@ __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict_
   if (fac) {
 #pragma unroll
     for (int g = 2; g < 4; ++g) {
-      int d[NSLICE][8];
-      digits8(&x[g * 8], er, &bad, d);
+      uint4 d[NSLICE];
+      digits8_packed(&x[g * 8], er, &bad, d);
 #pragma unroll
       for (int p = 0; p < NSLICE; ++p)
-        *reinterpret_cast<uint4*>(gbase + (size_t)p * SLICE_BYTES + (size_t)(kg0 + g) * 2048) = pack_half8(d[p]);
+        *reinterpret_cast<uint4*>(gbase + (size_t)p * SLICE_BYTES + (size_t)(kg0 + g) * 2048) = d[p];
     }
   }
   if (live) {
