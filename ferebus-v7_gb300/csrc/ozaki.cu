@@ -83,8 +83,9 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
 // TMEM columns.  Warp 8 (one lane) streams the digit planes of each k-chunk
 // of 16 by 5-D TMA into a 3-stage ring and bulk-copies the tile's
 // accumulators (96 KB) into shared memory as soon as the previous tile's
-// epilogue has released that buffer; warp 9 (one lane) issues the 28
-// tcgen05.mma of a chunk; warps 0-7 drain TMEM into registers, release it
+// epilogue has released that buffer; warp 9 (one lane) issues the
+// chunk's 28 digit pairs as 10 tcgen05.mma with B's planes stacked along N
+// (upd_issue_chunk); warps 0-7 drain TMEM into registers, release it
 // (so the next tile's MMAs start), then add the tile to the accumulators
 // and write them back to HBM while the tensor cores work on the next tile.
 //

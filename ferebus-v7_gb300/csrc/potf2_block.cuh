@@ -1,8 +1,8 @@
 // The W x W diagonal-block Cholesky (FP64) with its log-det part, as a
 // block-level device routine for W * 4 threads (W / 8 warps): called by its
 // own kernel (barrier 0 = the whole CTA) and by the tensor-core coupling
-// kernel, whose four epilogue warps factor the next quarter's diagonal block
-// as soon as they have coupled into it (barrier 1).
+// kernel, whose epilogue warps 0-3 factor the next quarter's diagonal block
+// as soon as the tile holding it is coupled (barrier 2).
 //
 // Right-looking, one column per step, the block held in registers: warp w
 // owns the columns c = w + NWARP * k (k < 8), lane l holds rows l + 32 h of
