@@ -199,6 +199,7 @@ int default_mode() {
 
 // Optional per-launch event pairs for stage timing (captured into the graph).
 struct StageEvents {
+  int only = -1;                // >= 0: time only the launches of this stage
   std::vector<int> stage;
   std::vector<cudaEvent_t> ev;  // 2 per launch
   void clear() {
@@ -384,7 +385,7 @@ int build_sched(const std::vector<int>& nt128, const std::vector<int>& tc_build,
 }
 
 int mark(StageEvents* pe, int stage, cudaStream_t s, bool begin) {
-  if (!pe) return 0;
+  if (!pe || (pe->only >= 0 && stage != pe->only)) return 0;
   cudaEvent_t e;
   CK(cudaEventCreate(&e));
   pe->ev.push_back(e);
@@ -1015,6 +1016,7 @@ void fgpu_plan_destroy(fgpu_plan* p) {
 int fgpu_plan_set_profiling(fgpu_plan* p, int enable) {
   t_err.clear();
   if (!p) return fail(FGPU_EINVAL, "plan is NULL");
+  if (enable < 0 || enable > 2) return fail(FGPU_EINVAL, "profiling mode must be 0, 1 or 2");
   CK(cudaSetDevice(p->device));
   std::lock_guard<std::mutex> lk(p->mu);
   CK(cudaStreamSynchronize(p->stream));
@@ -1023,7 +1025,10 @@ int fgpu_plan_set_profiling(fgpu_plan* p, int enable) {
     delete p->prof;
     p->prof = nullptr;
   }
-  if (enable) p->prof = new StageEvents();
+  if (enable) {
+    p->prof = new StageEvents();
+    if (enable == 2) p->prof->only = 3;  // the trailing update alone: two event nodes per step
+  }
   cudaGraphExec_t g = nullptr;
   long long nk = 0;
   int rc = capture(p->stream, &g, p->probs_d, p->nprob, p->max_nsteps, p->max_nplanes, p->status_all,

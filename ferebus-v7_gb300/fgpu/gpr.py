@@ -121,7 +121,10 @@ class Plan:
         return int(self.lib.fgpu_last_launch_count())
 
     def set_profiling(self, enable=True):
-        _lib.check(self.lib.fgpu_plan_set_profiling(self.handle, 1 if enable else 0))
+        """True: event nodes around every launch; "update": around the
+        trailing-update launches only; False: off."""
+        mode = 2 if enable == "update" else (1 if enable else 0)
+        _lib.check(self.lib.fgpu_plan_set_profiling(self.handle, mode))
 
     STAGES = ("build", "potf2", "trsm", "update", "finalize", "panel_prep", "split", "border", "coupling")
 

@@ -147,7 +147,9 @@ int fgpu_loglik_noalloc(int N, int d, const double* X_dev, const double* y_dev, 
                         const double* theta_dev, double* ll_dev, int* info_dev, void* stream);
 
 /* Stage timing for roofline accounting.  When enabled, the plan's graph is
- * re-captured with CUDA event nodes around every launch; after a run,
+ * re-captured with CUDA event nodes around every launch (enable = 1) or
+ * around the trailing-update launches only (enable = 2, which leaves the
+ * rest of the graph as it runs unprofiled); after a run,
  * fgpu_plan_stage_times fills ms[k] with the summed device time of stage k
  * during the LAST replay and count[k] with its launches (k: 0 build,
  * 1 diagonal factor, 2 panel solve, 3 trailing update, 4 likelihood
