@@ -323,6 +323,10 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
         const int eexp = 2 * P.fscale[d] + 1 - u;
         const long long wi = P.fnorm[(size_t)d * nc + i];
         const long long* wj = P.fnorm + (size_t)d * nc + j0;
+        // a plain sum of the two leaves (a = d = 0, b = c = 1) is one add,
+        // the same double as the general form
+        const bool plain_sum = d > 0 && P.fcoef[0] == 0.0 && P.fcoef[1] == 1.0 && P.fcoef[2] == 1.0 &&
+                               P.fcoef[3] == 0.0;
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
           long long E = wi + wj[q] - 2 * W[q];
@@ -330,6 +334,8 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
           const double val = iexp_fixed((unsigned long long)E, eexp);
           if (d == 0) {
             v0[q] = val;
+          } else if (plain_sum) {
+            v0[q] = v0[q] + val;
           } else {
             // second distance leaf: k = (d v0 + c) v1 + (b v0 + a)
             v0[q] = fma(fma(P.fcoef[3], v0[q], P.fcoef[2]), val, fma(P.fcoef[1], v0[q], P.fcoef[0]));
