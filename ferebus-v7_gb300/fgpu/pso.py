@@ -173,7 +173,10 @@ class LockstepPSO:
         """Relative-change stopping criterion (pso.f90:619-636)."""
         if self.cfg.stall_iterations <= 0:
             return False
-        if st.stall_cost != 0 and abs((st.gbest_cost - st.stall_cost) / st.stall_cost) <= self.cfg.tolerance:
+        # the first check divides by the initial infinite stall cost: NaN, which
+        # compares false in the reference, i.e. a reset
+        if (np.isfinite(st.stall_cost) and st.stall_cost != 0
+                and abs((st.gbest_cost - st.stall_cost) / st.stall_cost) <= self.cfg.tolerance):
             st.stall_count += 1
         else:
             st.stall_count = 0
