@@ -59,3 +59,6 @@ def test_argument_errors_need_no_device(lib):
     assert lib.fgpu_loglik(None, dp, 1, None, None, None) == -1
     assert lib.fgpu_plan_create(C.byref(h), None, 0, 1) == -1
     assert b"NULL" in lib.fgpu_last_error() or b"bad" in lib.fgpu_last_error()
+    for mode in (0, 1, 2):
+        assert lib.fgpu_plan_set_profiling(None, mode) == -1
+    assert b"NULL" in lib.fgpu_last_error()
