@@ -114,3 +114,84 @@ def loglik_from_factor(L, y, mu, likelihood):
     r = y - m
     s2 = float(r @ solve(r)) / n
     return -0.5 * n * math.log(s2) - 0.5 * logdet
+
+
+def couple(T, X, ex, Y, ey, levels=7):
+    """T -= round(sum_k X_ik Y_jk) from digit planes (the couplings inside a
+    panel): the exact level sums converted with one rounding, then
+    subtracted.  X: rows of T in their scales ex; Y: the coupled columns' L
+    rows in their scales ey."""
+    hi, lo = level_hi_lo(digits(X, ex), digits(Y, ey), levels)
+    w = hi.astype(np.float64) * 16777216.0 + lo
+    T -= np.ldexp(w, ex[:, None] + ey[None, :] - 62)
+
+
+def panel_solve(B, Lqq, eb, eq, pieces=2, levels=7):
+    """X Lqq^T = B for the rows below a 32 x 32 diagonal block: FP64
+    substitution in pieces of 32 / pieces columns, the later pieces coupled
+    to the earlier ones on digit planes.  pieces = 2: the engine's two
+    halves, one coupling; pieces = 4: 8-column pieces with couplings
+    0 -> 1, (0, 1) -> (2, 3), 2 -> 3."""
+    X = B.copy()
+    w = 32 // pieces
+
+    def solve(p):
+        c = slice(p * w, (p + 1) * w)
+        X[:, c] = sla.solve_triangular(Lqq[c, c], X[:, c].T, lower=True).T
+
+    if pieces == 2:
+        solve(0)
+        couple(X[:, 16:], X[:, :16], eb, Lqq[16:, :16], eq[16:], levels)
+        solve(1)
+    elif pieces == 4:
+        solve(0)
+        couple(X[:, 8:16], X[:, :8], eb, Lqq[8:16, :8], eq[8:16], levels)
+        solve(1)
+        couple(X[:, 16:], X[:, :16], eb, Lqq[16:, :16], eq[16:], levels)
+        solve(2)
+        couple(X[:, 24:], X[:, 16:24], eb, Lqq[24:, 16:24], eq[24:], levels)
+        solve(3)
+    else:
+        raise ValueError(pieces)
+    return X
+
+
+def factor_quarters(K, pieces=2, levels=7):
+    """As `factor`, with the panel worked as the engine works it: four
+    32-column quarters (FP64 diagonal factor, panel solve in pieces) and the
+    digit-plane couplings quarter 0 -> 1, half 0 -> half 1, quarter 2 -> 3."""
+    n = K.shape[0]
+    nc = -(-n // NB) * NB
+    A = np.eye(nc)
+    A[:n, :n] = np.tril(K)
+    e = row_scales(A)
+    acc_hi = np.zeros((nc, nc), dtype=np.int64)
+    acc_lo = np.zeros((nc, nc), dtype=np.int64)
+    for c0 in range(0, nc, NB):
+        c1 = c0 + NB
+        if c0 > 0:
+            w = acc_hi[c0:, c0:c1].astype(np.float64) * 16777216.0 + acc_lo[c0:, c0:c1]
+            A[c0:, c0:c1] -= np.ldexp(w, e[c0:, None] + e[None, c0:c1] - 62)
+        for q in range(4):
+            a = c0 + 32 * q
+            b = a + 32
+            if q == 1:
+                couple(A[a:, a:b], A[a:, c0:a], e[a:], A[a:b, c0:a], e[a:b], levels)
+            elif q == 2:
+                couple(A[a:, a:c1], A[a:, c0:a], e[a:], A[a:c1, c0:a], e[a:c1], levels)
+            elif q == 3:
+                couple(A[a:, a:b], A[a:, c0 + 64:a], e[a:], A[a:b, c0 + 64:a], e[a:b], levels)
+            Lqq, info = lapack.dpotrf(A[a:b, a:b], lower=1, clean=1)
+            if info != 0:
+                return None, int(info) + a
+            A[a:b, a:b] = Lqq
+            if b < nc:
+                A[b:, a:b] = panel_solve(A[b:, a:b], Lqq, e[b:], e[a:b], pieces, levels)
+        if c1 < nc:
+            D = digits(A[c1:, c0:c1], e[c1:])
+            hi, lo = level_hi_lo(D, D, levels)
+            acc_hi[c1:, c1:] += hi
+            acc_lo[c1:, c1:] += lo
+            acc_hi[c1:, c1:] += acc_lo[c1:, c1:] >> 24
+            acc_lo[c1:, c1:] &= 0xFFFFFF
+    return np.tril(A[:n, :n]), 0

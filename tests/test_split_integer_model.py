@@ -7,7 +7,9 @@ element).  With the engine's 7 levels every golden case's log-likelihood
 meets the parity tolerance against the oracle's LAPACK value; with fewer
 levels some do not, which shows that the test can fail and that 7 is the
 smallest level count the fixtures accept (measured: 6 levels miss the
-ammonia set by ~2400x its tolerance, 5 levels by ~4e4x).
+ammonia set by ~2400x its tolerance, 5 levels by ~4e4x).  A second model
+(`factor_quarters`) also restates the engine's work inside a panel: the
+32-column quarters with digit-plane couplings between and within them.
 """
 import numpy as np
 import pytest
@@ -17,8 +19,9 @@ from conftest import golden_cases, load_case
 from oracle import gpr_oracle as O
 
 
-def _worst_ratio(name, levels):
-    """max over the case's PD thetas of |ll_model - ll_oracle| / tolerance."""
+def _worst_ratio(name, levels, quarters=False):
+    """max over the case's PD thetas of |ll_model - ll_oracle| / tolerance;
+    `quarters`: the panel worked in the engine's quarters and halves."""
     c = load_case(name)
     ks = [int(v) for v in c["kspec"]]
     nk = O.kernel_nparams(ks)
@@ -29,7 +32,7 @@ def _worst_ratio(name, levels):
             continue
         noise = float(th[nk]) if int(c["optimise_noise"]) else float(c["noise"])
         K = O.compute_R(ks, th[:nk], noise, tens)
-        L, info = M.factor(K, levels)
+        L, info = M.factor_quarters(K, 2, levels) if quarters else M.factor(K, levels)
         if info != 0:
             return np.inf, compared
         ll = M.loglik_from_factor(L, c["y"], c["mu"], int(c["likelihood"]))
@@ -42,6 +45,16 @@ def _worst_ratio(name, levels):
 @pytest.mark.parametrize("name", [n for n in golden_cases() if "not_pd" not in n])
 def test_scheme_meets_parity_tolerance(name):
     worst, compared = _worst_ratio(name, 7)
+    assert compared > 0
+    assert worst <= 1.0, worst
+
+
+@pytest.mark.parametrize("name", [n for n in golden_cases() if "not_pd" not in n])
+def test_scheme_with_the_engines_panel_structure_meets_parity_tolerance(name):
+    """The same with the panel worked as the engine works it: 32-column
+    quarters, each quarter's panel solve in two halves coupled on digit
+    planes, and the digit couplings quarter 0 -> 1, half 0 -> 1, 2 -> 3."""
+    worst, compared = _worst_ratio(name, 7, quarters=True)
     assert compared > 0
     assert worst <= 1.0, worst
 
