@@ -10,15 +10,25 @@ one PSO iteration's swarm evaluated in one graph-captured batched pass.
                 (device-pointer entry point), max time over ranks.
 * e2e         : the same metric through the public batched C-ABI call with
                 host buffers (theta H2D and ll/info D2H inside the timed region).
-* plain       : evaluations/s of the one-particle-per-call drop-in.
-* roofline    : the dominant kernel's (trailing update, FP64 MMA) achieved
-                FP64 rate over its CUDA-event time inside the timed region,
-                against FP64 peak measured live (cuBLAS DGEMM).
+* plain       : evaluations/s of the one-particle-per-call drop-in
+                (fgpu_loglik), over 40 particles.
+* roofline    : the dominant kernel, the tensor-core trailing update
+                (k_ozaki_update): the fp16 tensor flops it issues (7 digit
+                planes, 28 digit pairs per 128 x 64 x 128 tile) over its
+                CUDA-event time inside the timed region, against the measured
+                sustained bf16 peak (MEASURED_PEAKS.json); its FP64-equivalent
+                rate is set beside the FP64 DGEMM peak measured live.
+                `traffic` is scaled from the committed ncu capture
+                (profiles/traffic.json: DRAM bytes per 128 x 64 tile) to the
+                tiles of one launch.
+* build       : the kernel-matrix build's algorithmic HBM bytes
+                (8 N(N+1)/2 written + 8 N d + 8 N read per evaluation) over the
+                build stage's time, against the measured HBM bandwidth.
 * cpu_baseline: the C restatement of the reference's OpenMP CPU path on a
                 bounded sample of particles, all host cores.
 Inputs are larger than L2: each step writes 40 K matrices (5.3 GB).
 ``--impl reference`` times only the CPU restatement (the reference itself is
-Fortran and cannot be built on these machines).
+Fortran and cannot be built on these machines), on the same workload.
 """
 from __future__ import annotations
 
@@ -173,6 +183,14 @@ def host_info():
     return os.cpu_count(), model
 
 
+def workload_config(p, S, ws):
+    """The `config` object of both arms' JSON lines."""
+    return {"workload": WORKLOAD, "N": p.N, "d": p.d, "swarm": S, "likelihood": "concentrated",
+            "kernel": "rbf(17) + periodic(7)",
+            "l2": "inputs larger than L2: 40 K matrices = 5.3 GB written per step",
+            "parallelism": f"replicas x{ws} (independent swarms per GPU)"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if ws > 1:
@@ -203,17 +221,130 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, shapes of the glycine-like config)",
-            "config": {"workload": WORKLOAD, "N": p.N, "d": p.d, "swarm_sample_per_step": sample},
+            "config": workload_config(p, args.swarm, ws),
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{sample} particles per step ({model}); C restatement of the "
-                                       "reference's OpenMP path (distance tensors + dgemv + dpotrf/dpotrs)"},
+                             "sample": f"{sample} of the swarm's particles per step ({model}); C restatement of "
+                                       "the reference's OpenMP path (distance tensors + dgemv + dpotrf/dpotrs)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.barrier()
         dist.destroy_process_group()
+
+
+def host_mem_available():
+    try:
+        for ln in open("/proc/meminfo"):
+            if ln.startswith("MemAvailable:"):
+                return int(ln.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def shape_problems(key):
+    """(problems, swarm size, description) of one benchmark shape."""
+    from fgpu import synth
+    if key == "water_like_500":
+        return [synth.config1()], 20, "water-like: N=500, d=3, rbf(1,2)+periodic(3), constant mean, marginal, S=20"
+    if key == "methanol_like_2000":
+        return [synth.config2()], 50, "methanol-like: N=2000, d=12, rbf(1-9)+periodic(10-12), marginal, S=50"
+    if key == "atoms_33_ragged":
+        return synth.config4(), 30, ("33 atoms, N ~ U{500..6000}, d=93, rbf+periodic(30 dihedrals), linear mean, "
+                                     "marginal, 30 particles each: 990 problems per step")
+    if key == "large_n_10000":
+        return [synth.config5()], 16, ("large-N: N=10000, d=30, rbf+periodic, quadratic mean, optimised noise "
+                                       "in [1e-12, 1e-6], S=16")
+    raise KeyError(key)
+
+
+def measure_shape(key, torch, stream, steps, warmup, tpeak, cores, cpu_model, no_cpu):
+    """Throughput, end-to-end rate, update roofline and a bounded CPU sample
+    of one benchmark shape: every particle of every problem in one batch plan."""
+    from fgpu import Engine, Plan
+    from fgpu.gpr import mean_vector
+    probs, S, desc = shape_problems(key)
+    mus = [mean_vector(q.mean, q.X, q.y) for q in probs]
+    engines = [Engine(q.X, q.y, mu, q.kspec, q.likelihood, q.noise, q.optimise_noise) for q, mu in zip(probs, mus)]
+    flat = [e for e in engines for _ in range(S)]
+    nth = max(e.ntheta for e in engines)
+    plan = Plan(flat, ldtheta=nth)
+    nwaves, arena = plan.waves()
+    total = warmup + steps
+    th = np.zeros((total, len(flat), nth))
+    for a, q in enumerate(probs):
+        t = q.thetas(S * total, seed=40 + a).reshape(total, S, q.ntheta)
+        th[:, a * S:(a + 1) * S, :q.ntheta] = t
+    th_dev = torch.tensor(th, dtype=torch.float64, device="cuda")
+    ll_dev = torch.empty((total, len(flat)), dtype=torch.float64, device="cuda")
+    info_dev = torch.empty((total, len(flat)), dtype=torch.int32, device="cuda")
+    plan.set_profiling("update")
+
+    def step(k):
+        plan.run_device(th_dev[k].data_ptr(), ll_dev[k].data_ptr(), info_dev[k].data_ptr(), stream.cuda_stream)
+
+    for w in range(warmup):
+        step(w)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(steps):
+        step(warmup + k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    upd_ms, upd_n = plan.stage_times()["update"]
+    launches = plan.launches()
+    fail = float(np.mean(info_dev[warmup:].cpu().numpy() != 0))
+    plan.set_profiling(False)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        plan.run(th[warmup + k])
+    e2e_s = (time.perf_counter() - t0) / steps
+    tflops = sum(tensor_update_flops(q.N) * S for q in probs)
+    achieved = tflops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
+    out = {"workload": desc, "problems_per_step": len(flat), "value": len(flat) / (ms * 1e-3), "unit": UNIT,
+           "ms_per_step": ms, "waves": nwaves, "workspace_arena_gb": arena / 1e9,
+           "e2e": {"value": len(flat) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": len(flat) * nth * 8,
+                   "d2h_bytes_per_step": len(flat) * 12},
+           "roofline": {"bound": "tensor", "kernel": "k_ozaki_update", "achieved": achieved, "peak": tpeak,
+                        "unit": "TFLOP/s", "frac": achieved / tpeak if achieved else None,
+                        "update_ms_per_step": upd_ms, "update_launches": upd_n},
+           "gpu_launches": launches * steps, "cholesky_failure_rate": fail}
+    del plan, th_dev, ll_dev, info_dev
+    for e in engines:
+        e.close()
+    if no_cpu:
+        return out
+    # bounded CPU sample: one particle per core of up to three problems (for
+    # the ragged batch the atoms at the 10th, 50th and 90th size percentile,
+    # skipping any whose d x N x N distance tensors would not fit in host memory)
+    from oracle.build_ref import RefCPU
+    order = sorted(range(len(probs)), key=lambda a: probs[a].N)
+    pick = sorted({order[int(f * (len(order) - 1))] for f in (0.1, 0.5, 0.9)}) if len(probs) > 1 else [0]
+    avail = host_mem_available()
+    done, secs, names = 0, 0.0, []
+    for a in pick:
+        q = probs[a]
+        need = 2 * 8.0 * q.d * q.N * q.N
+        if avail and need > 0.4 * avail:
+            names.append(f"N={q.N} skipped ({need / 1e9:.0f} GB of tensors)")
+            continue
+        ref = RefCPU(q.X, q.y, mus[a], q.kspec, q.likelihood, q.noise, q.optimise_noise)
+        t = q.thetas(cores, seed=77)
+        t0 = time.perf_counter()
+        ref.loglik_batch(t, cores)
+        secs += time.perf_counter() - t0
+        ref.close()
+        done += cores
+        names.append(f"N={q.N}")
+    if done:
+        out["cpu_baseline"] = {"value": done / secs, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"{done} particles ({', '.join(names)}), one per core, in {secs:.1f} s "
+                                         f"({cpu_model}); C restatement of the reference's OpenMP CPU path"}
+    return out
 
 
 def main():
@@ -223,12 +354,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fgpu", choices=("fgpu", "reference"))
     ap.add_argument("--swarm", type=int, default=40)
-    ap.add_argument("--plain", type=int, default=4, help="particles timed on the plain path")
+    ap.add_argument("--plain", type=int, default=40, help="particles timed on the plain path")
     ap.add_argument("--cpu-sample", type=int, default=0, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--trailing", default="tcgen05", choices=("tcgen05", "fp64"),
                     help="trailing-update arithmetic of the Cholesky")
+    ap.add_argument("--shapes", default="water_like_500,methanol_like_2000,atoms_33_ragged,large_n_10000",
+                    help="other benchmark shapes measured after the headline ('none' to skip)")
+    ap.add_argument("--shape-steps", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -320,6 +454,17 @@ def main():
         eng.loglik(th_host[args.warmup][k % S])
     plain_v = args.plain / (time.perf_counter() - t0)
 
+    # the FP64 adjoint (gradient polish) at the same shape, one particle:
+    # algorithmic FP64 work N^3 (Cholesky N^3/3, triangular inverse N^3/3,
+    # K^-1 = L^-T L^-1 N^3/3) + the fused dK pass (~10 flops per entry and dim)
+    eng.grad(th_host[0][0])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(2):
+        eng.grad(th_host[args.warmup][k])
+    grad_s = (time.perf_counter() - t0) / 2
+    grad_flops = float(p.N) ** 3 + 10.0 * p.N * (p.N + 1) / 2 * p.d
+
     # per-stage breakdown (diagnostic): one more, untimed replay with event
     # nodes around every launch
     plan.set_profiling(True)
@@ -346,9 +491,19 @@ def main():
         except Exception:
             traffic = None
     stage_ms = {k: v[0] for k, v in breakdown.items() if v[1]}
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
+    # the kernel-matrix build against HBM: algorithmic bytes per evaluation
+    # (lower triangle of K written, X and y / mu read) over the build stage
+    build_bytes = S * (8.0 * p.N * (p.N + 1) / 2 + 8.0 * p.N * p.d + 8.0 * p.N)
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    build_ms = stage_ms.get("build")
+    build = {"bytes_per_step": build_bytes, "ms_per_step": build_ms,
+             "achieved_gbs": build_bytes / (build_ms * 1e-3) / 1e9 if build_ms else None,
+             "peak_gbs": hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks.get("hbm_gbs")
+             else "fallback 6.8 TB/s (profiling recipe)"}
+    build["hbm_frac"] = build["achieved_gbs"] / hbm if build["achieved_gbs"] else None
     if mode == "tcgen05":
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
         tpeak = peaks.get("bf16_tflops_sustained")
         src = "MEASURED_PEAKS.json bf16_tflops_sustained (dense fp16/bf16 tensor, kernel timed inside a long step)"
         if not tpeak:
@@ -357,6 +512,8 @@ def main():
         achieved = tflops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
         roof = {"bound": "tensor", "achieved": achieved, "peak": tpeak, "unit": "TFLOP/s",
                 "frac": (achieved / tpeak) if achieved else None, "traffic": traffic,
+                "traffic_source": "DRAM bytes per 128 x 64 tile from the committed ncu capture "
+                                  "(profiles/traffic.json) x tiles per launch; not measured in this run",
                 "kernel": "k_ozaki_update (tcgen05.mma kind::f16, 7 fp16 digit planes, exact int64 accumulation)",
                 "peak_source": src, "tensor_flops_per_step": tflops, "launches_per_step": upd_n,
                 "fp64_equivalent": {"achieved": fp64_equiv, "fp64_peak": fp64_peak, "unit": "TFLOP/s",
@@ -382,17 +539,29 @@ def main():
         except Exception as exc:  # report, never fall back
             cpu = {"value": None, "unit": UNIT, "cores": cores, "kind": "port", "sample": f"failed: {exc}"}
     clocks = clk.summary()
+    shapes = {}
+    if rank == 0 and mode == "tcgen05" and args.shapes != "none":
+        cores, cpu_model = host_info()
+        for key in args.shapes.split(","):
+            try:
+                shapes[key] = measure_shape(key, torch, stream, args.shape_steps, 3, tpeak, cores, cpu_model,
+                                            args.no_cpu)
+            except Exception as exc:  # report, never fall back
+                shapes[key] = {"error": f"{type(exc).__name__}: {exc}"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, shapes of the glycine-like config)",
-            "config": {"workload": WORKLOAD, "N": p.N, "d": p.d, "swarm": S, "likelihood": "concentrated",
-                       "trailing_update": mode,
-                       "kernel": "rbf(17) + periodic(7)", "l2": "inputs larger than L2: 40 K matrices = 5.3 GB "
-                       "written per step", "parallelism": f"replicas x{ws} (independent swarms per GPU)"},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "config": workload_config(p, S, ws),
+            "trailing_update": mode,
+            "roofline": roof, "build": build, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
             "plain": {"value": plain_v, "unit": UNIT, "particles": args.plain},
+            "grad": {"ms": grad_s * 1e3, "fp64_flops": grad_flops,
+                     "fp64_tflops": grad_flops / grad_s / 1e12, "fp64_peak_tflops": fp64_peak,
+                     "frac": grad_flops / grad_s / 1e12 / fp64_peak,
+                     "what": "fgpu_grad (d logL / d theta, FP64 adjoint), one particle, host wall clock"},
             "batched_over_plain": value / ws / plain_v if plain_v else None,
+            "shapes": shapes,
             "cholesky_failure_rate": fail_rate}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -4,6 +4,7 @@
 #include "../../include/fgpu.h"
 #include "fgpu_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -14,6 +15,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 using namespace fgpu;
@@ -165,7 +167,12 @@ void free_sched_sync(UpdSched& u) {
   u.side = nullptr;
 }
 
+// One problem's device buffers.  They are carved from one block (`base`,
+// owned by a worker; a batch plan carves them from its shared arena instead
+// and leaves `base` null); the TMA tensor maps live in their own 512 bytes
+// because they must outlive the arena's reuse by later waves of a plan.
 struct Workspace {
+  void* base = nullptr;
   double* K = nullptr;
   double* logdet_part = nullptr;
   int* status = nullptr;
@@ -259,9 +266,25 @@ struct fgpu_ctx {
   std::vector<Worker*> workers;
 };
 
+// A batch plan.  Its problems run in waves (each wave one pass of the
+// kernels over its problems; the waves one after the other in the same
+// graph) whose workspaces share one arena: a batch whose workspaces do not
+// fit the device memory budget at once still runs in one graph replay.
+// probs_d holds the problems in wave order; order[k] is the caller's index
+// of wave-order problem k (outputs land at the caller's index).
+struct PlanWave {
+  int first = 0, count = 0;  // range of probs_d
+  int max_nsteps = 0, max_nplanes = 0;
+  size_t bytes = 0;          // arena bytes this wave's workspaces span
+  UpdSched sched;
+};
+
 struct fgpu_plan {
-  int device = 0, nprob = 0, ldtheta = 0, max_nsteps = 0, max_nplanes = 0, mode = 0;
+  int device = 0, nprob = 0, ldtheta = 0, mode = 0;
   std::vector<fgpu_ctx*> ctxs;
+  std::vector<int> order;
+  std::vector<PlanWave> waves;
+  size_t arena_bytes = 0;
   std::vector<Prob> probs_h;
   Prob* probs_d = nullptr;
   double* theta_d = nullptr;
@@ -276,7 +299,6 @@ struct fgpu_plan {
   double* h_ll = nullptr;
   int* h_info = nullptr;
   StageEvents* prof = nullptr;
-  UpdSched sched;
   std::mutex mu;
 };
 
@@ -498,36 +520,157 @@ int capture(cudaStream_t s, cudaGraphExec_t* exec, const Prob* probs_d, int npro
   return 0;
 }
 
-int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track) {
-  CK(cudaMalloc(&ws.K, K_elems(c) * sizeof(double)));
-  // one log-det part per 64-column block (FP64 mode) or 32-column quarter (tensor-core mode)
-  CK(cudaMalloc(&ws.logdet_part, sizeof(double) * 2 * (c->nsteps + 1)));
-  CK(cudaMalloc(&ws.out, sizeof(double) * 8));
-  CK(cudaMalloc(&ws.z, sizeof(double) * c->Nc));
-  if (c->mode == 1) {
-    const size_t nc = (size_t)c->Nc;
-    CK(cudaMalloc(&ws.escale, sizeof(int) * nc));
-    CK(cudaMalloc(&ws.pw2, sizeof(double) * nc));
-    CK(cudaMalloc(&ws.acc_hi, sizeof(long long) * nc * nc));
-    CK(cudaMalloc(&ws.acc_lo, sizeof(int) * nc * nc));
-    CK(cudaMalloc(&ws.slices, (size_t)c->nt128 * NSLICE * SLICE_BYTES));
-    CK(cudaMalloc(&ws.splanes, sizeof(double) * (size_t)std::max(c->spec.nplanes, 1) * nc));
-    CK(cudaMalloc(&ws.norms, sizeof(double) * (size_t)MAX_LEAF * nc));
-    CK(cudaMemset(ws.norms, 0, sizeof(double) * (size_t)MAX_LEAF * nc));
-    CK(cudaMalloc(&ws.fnorm, sizeof(long long) * 2 * nc));
-    CK(cudaMalloc(&ws.fcoef, sizeof(double) * 4));
-    CK(cudaMalloc(&ws.fscale, sizeof(int) * 2));
-    CK(cudaMalloc(&ws.tmaps, 512));
-    alignas(64) unsigned char maps[512];
-    const int er = encode_slice_maps(maps, ws.slices, c->nt128);
-    if (er != 0) return fail(FGPU_ECUDA, "cuTensorMapEncodeTiled failed (%d)", er);
-    CK(cudaMemcpy(ws.tmaps, maps, 512, cudaMemcpyHostToDevice));
+// Split a batch into waves whose workspaces fit `budget` bytes together.
+// If the whole batch fits it is one wave in the caller's order; otherwise
+// the problems are taken in decreasing workspace size and each wave is
+// filled first-fit (a problem joins the current wave while it fits, else
+// opens the next), so the largest problems share the first waves and the
+// small ones pack densely into the last.  Returns FGPU_ENOMEM (message
+// set) if a single problem exceeds the budget.
+int plan_waves(const std::vector<size_t>& bytes, size_t budget, std::vector<std::vector<int>>& groups) {
+  groups.clear();
+  const int n = (int)bytes.size();
+  size_t total = 0;
+  for (size_t b : bytes) total += b;
+  if (total <= budget) {
+    groups.emplace_back();
+    for (int i = 0; i < n; ++i) groups.back().push_back(i);
+    return 0;
   }
-  if (track) {
-    for (void* q : {(void*)ws.K, (void*)ws.logdet_part, (void*)ws.out, (void*)ws.z, (void*)ws.escale,
-                    (void*)ws.pw2, (void*)ws.acc_hi, (void*)ws.acc_lo, (void*)ws.slices, (void*)ws.tmaps,
-                    (void*)ws.splanes, (void*)ws.norms, (void*)ws.fnorm, (void*)ws.fcoef, (void*)ws.fscale})
-      if (q) track->push_back(q);
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return bytes[a] > bytes[b]; });
+  size_t cur = 0;
+  for (int i : idx) {
+    if (bytes[i] > budget)
+      return fail(FGPU_ENOMEM, "problem %d needs %zu bytes of workspace; the device budget is %zu", i, bytes[i],
+                  budget);
+    if (groups.empty() || cur + bytes[i] > budget) {
+      groups.emplace_back();
+      cur = 0;
+    }
+    groups.back().push_back(i);
+    cur += bytes[i];
+  }
+  return 0;
+}
+
+// Device memory a plan's workspaces may take at once: the environment
+// variable FGPU_PLAN_MEM_BUDGET_MB if set, else the free memory less a
+// reserve of max(1 GiB, 4 % of the device) for everything else.
+size_t plan_memory_budget() {
+  if (const char* v = getenv("FGPU_PLAN_MEM_BUDGET_MB")) {
+    const double mb = atof(v);
+    if (mb > 0) return (size_t)(mb * 1048576.0);
+  }
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    return (size_t)-1;  // unknown: one wave, and allocation reports the shortfall
+  }
+  const size_t reserve = std::max((size_t)1 << 30, tot / 25);
+  return fr > reserve ? fr - reserve : 0;
+}
+
+// Capture a plan's waves, one after the other on the plan's stream, into
+// one graph.
+int capture_plan(fgpu_plan* p, cudaGraphExec_t* exec, long long* kernels, StageEvents* pe) {
+  cudaStream_t s = p->stream;
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = 0;
+  long long total = 0;
+  for (PlanWave& w : p->waves) {
+    long long n = 0;
+    rc = enqueue_eval(p->probs_d + w.first, w.count, w.max_nsteps, w.max_nplanes, p->status_all + 4 * w.first,
+                      sizeof(int) * 4 * w.count, s, &n, pe, p->mode, p->mode == 1 ? &w.sched : nullptr);
+    if (rc) break;
+    total += n;
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (rc != 0) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(FGPU_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(FGPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  if (kernels) *kernels = total;
+  return 0;
+}
+
+// Carve one problem's buffers from `base` (256-byte aligned pieces) and
+// return the bytes they span; with base == nullptr only the size is
+// computed.  The block needs no clearing: every buffer is written by the
+// evaluation before it is read.
+size_t layout_workspace(const fgpu_ctx* c, unsigned char* base, Workspace& ws) {
+  size_t off = 0;
+  auto take = [&](auto*& dst, size_t bytes) {
+    off = (off + 255) / 256 * 256;
+    dst = base ? reinterpret_cast<std::remove_reference_t<decltype(dst)>>(base + off) : nullptr;
+    off += bytes;
+  };
+  const size_t nc = (size_t)c->Nc;
+  take(ws.K, K_elems(c) * sizeof(double));
+  // one log-det part per 64-column block (FP64 mode) or 32-column quarter (tensor-core mode)
+  take(ws.logdet_part, sizeof(double) * 2 * (c->nsteps + 1));
+  take(ws.out, sizeof(double) * 8);
+  take(ws.z, sizeof(double) * nc);
+  if (c->mode == 1) {
+    take(ws.escale, sizeof(int) * nc);
+    take(ws.pw2, sizeof(double) * nc);
+    take(ws.acc_hi, sizeof(long long) * acc_tiles(c->nt128) * ACC_TILE_ELEMS);
+    take(ws.acc_lo, sizeof(int) * acc_tiles(c->nt128) * ACC_TILE_ELEMS);
+    take(ws.slices, (size_t)c->nt128 * NSLICE * SLICE_BYTES);
+    take(ws.splanes, sizeof(double) * (size_t)std::max(c->spec.nplanes, 1) * nc);
+    take(ws.norms, sizeof(double) * (size_t)MAX_LEAF * nc);
+    take(ws.fnorm, sizeof(long long) * 2 * nc);
+    take(ws.fcoef, sizeof(double) * 4);
+    take(ws.fscale, sizeof(int) * 2);
+  }
+  return (off + 255) / 256 * 256;
+}
+
+size_t workspace_bytes(const fgpu_ctx* c) {
+  Workspace tmp;
+  return layout_workspace(c, nullptr, tmp);
+}
+
+// Encode the problem's four TMA tensor maps over ws.slices into the 512
+// device bytes at `dst` (tensor-core mode only).
+int write_tmaps(const fgpu_ctx* c, const Workspace& ws, unsigned char* dst) {
+  if (c->mode != 1) return 0;
+  alignas(64) unsigned char maps[512];
+  const int er = encode_slice_maps(maps, ws.slices, c->nt128);
+  if (er != 0) return fail(FGPU_ECUDA, "cuTensorMapEncodeTiled failed (%d)", er);
+  CK(cudaMemcpy(dst, maps, 512, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// A worker's own workspace: one block plus its tensor maps.  On failure
+// nothing stays allocated and ws is left empty.
+int alloc_workspace(const fgpu_ctx* c, Workspace& ws) {
+  const size_t bytes = workspace_bytes(c);
+  void* base = nullptr;
+  cudaError_t e = cudaMalloc(&base, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // an allocation failure is not sticky; clear it
+    return fail(e == cudaErrorMemoryAllocation ? FGPU_ENOMEM : FGPU_ECUDA,
+                "workspace allocation of %zu bytes (N=%d): %s", bytes, c->N, cudaGetErrorString(e));
+  }
+  layout_workspace(c, static_cast<unsigned char*>(base), ws);
+  ws.base = base;
+  if (c->mode == 1) {
+    e = cudaMalloc(&ws.tmaps, 512);
+    int rc = e == cudaSuccess ? write_tmaps(c, ws, ws.tmaps)
+                              : fail(FGPU_ENOMEM, "tensor-map allocation: %s", cudaGetErrorString(e));
+    if (rc) {
+      cudaFree(ws.tmaps);
+      cudaFree(base);
+      ws = Workspace{};
+      return rc;
+    }
   }
   return 0;
 }
@@ -535,22 +678,9 @@ int alloc_workspace(const fgpu_ctx* c, Workspace& ws, std::vector<void*>* track)
 void free_worker(Worker* w) {
   if (!w) return;
   if (w->graph) cudaGraphExecDestroy(w->graph);
-  cudaFree(w->ws.K);
-  cudaFree(w->ws.logdet_part);
+  cudaFree(w->ws.base);
   cudaFree(w->ws.status);
-  cudaFree(w->ws.out);
-  cudaFree(w->ws.z);
-  cudaFree(w->ws.escale);
-  cudaFree(w->ws.pw2);
-  cudaFree(w->ws.acc_hi);
-  cudaFree(w->ws.acc_lo);
-  cudaFree(w->ws.slices);
   cudaFree(w->ws.tmaps);
-  cudaFree(w->ws.splanes);
-  cudaFree(w->ws.norms);
-  cudaFree(w->ws.fnorm);
-  cudaFree(w->ws.fcoef);
-  cudaFree(w->ws.fscale);
   cudaFree(w->theta_d);
   cudaFree(w->prob_d);
   cudaFree(w->sched.prefix_dev);
@@ -573,7 +703,7 @@ int make_worker(fgpu_ctx* c, Worker** out) {
   };
   if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(FGPU_ECUDA, "stream create failed"));
-  if ((rc = alloc_workspace(c, w->ws, nullptr)) != 0) return bail(rc);
+  if ((rc = alloc_workspace(c, w->ws)) != 0) return bail(rc);
   if (cudaMalloc(&w->ws.status, sizeof(int) * 4) != cudaSuccess) return bail(fail(FGPU_ENOMEM, "status alloc"));
   if (cudaMalloc(&w->theta_d, sizeof(double) * (c->ntheta + 1)) != cudaSuccess)
     return bail(fail(FGPU_ENOMEM, "theta alloc"));
@@ -618,8 +748,23 @@ void release(fgpu_ctx* c, Worker* w) {
   w->busy = false;
 }
 
+// Plans that fgpu_loglik_batch built, keyed by the context list, least
+// recently used first out: at most FGPU_PLAN_CACHE (default 8) are kept.
+// Entries are shared, so an evicted plan is destroyed only after the last
+// call still running it returns.
+struct CachedPlan {
+  std::shared_ptr<fgpu_plan> plan;
+  unsigned long long used = 0;
+};
 std::mutex g_plan_mu;
-std::map<std::vector<fgpu_ctx*>, fgpu_plan*> g_plans;
+std::map<std::vector<fgpu_ctx*>, CachedPlan> g_plans;
+unsigned long long g_plan_clock = 0;
+
+size_t plan_cache_limit() {
+  const char* v = getenv("FGPU_PLAN_CACHE");
+  const int n = v ? atoi(v) : 8;
+  return (size_t)(n > 0 ? n : 1);
+}
 
 }  // namespace
 
@@ -748,12 +893,13 @@ int fgpu_set_trailing_update(int mode) {
 void fgpu_destroy(fgpu_ctx* ctx) {
   if (!ctx) return;
   {
+    std::vector<std::shared_ptr<fgpu_plan>> drop;  // destroyed outside the lock
     std::lock_guard<std::mutex> lk(g_plan_mu);
     for (auto it = g_plans.begin(); it != g_plans.end();) {
       bool uses = false;
       for (fgpu_ctx* c : it->first) uses |= (c == ctx);
       if (uses) {
-        fgpu_plan_destroy(it->second);
+        drop.push_back(std::move(it->second.plan));
         it = g_plans.erase(it);
       } else {
         ++it;
@@ -926,72 +1072,105 @@ int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, double
 int fgpu_plan_create(fgpu_plan** out, fgpu_ctx* const* ctxs, int nprob, int ldtheta) {
   t_err.clear();
   if (!out || !ctxs || nprob < 1) return fail(FGPU_EINVAL, "bad plan arguments");
+  if (nprob > 65535) return fail(FGPU_EINVAL, "a plan holds at most 65535 problems (%d given)", nprob);
   *out = nullptr;
   std::unique_ptr<fgpu_plan> p(new (std::nothrow) fgpu_plan());
   if (!p) return fail(FGPU_ENOMEM, "plan allocation");
   p->nprob = nprob;
-  p->device = ctxs[0]->device;
+  p->device = ctxs[0] ? ctxs[0]->device : 0;
   int maxth = 0;
   for (int i = 0; i < nprob; ++i) {
     if (!ctxs[i]) return fail(FGPU_EINVAL, "ctxs[%d] is NULL", i);
     if (ctxs[i]->device != p->device) return fail(FGPU_EINVAL, "plan spans devices");
     maxth = std::max(maxth, ctxs[i]->ntheta);
     if (ctxs[i]->mode != ctxs[0]->mode) return fail(FGPU_EINVAL, "plan mixes trailing-update modes");
-    p->max_nsteps = std::max(p->max_nsteps, ctxs[i]->nsteps);
-    p->max_nplanes = std::max(p->max_nplanes, ctxs[i]->spec.nplanes);
     p->ctxs.push_back(ctxs[i]);
   }
   if (ldtheta < maxth) return fail(FGPU_EINVAL, "ldtheta=%d < max nparams %d", ldtheta, maxth);
   p->ldtheta = ldtheta;
-  CK(cudaSetDevice(p->device));
-  auto track = [&](void* q) { p->allocations.push_back(q); };
-  CK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
-  CK(cudaMalloc(&p->theta_d, sizeof(double) * (size_t)nprob * ldtheta));
-  track(p->theta_d);
-  CK(cudaMalloc(&p->ll_d, sizeof(double) * nprob));
-  track(p->ll_d);
-  CK(cudaMalloc(&p->info_d, sizeof(int) * nprob));
-  track(p->info_d);
-  CK(cudaMalloc(&p->status_all, sizeof(int) * 4 * nprob));
-  track(p->status_all);
-  CK(cudaMalloc(&p->probs_d, sizeof(Prob) * nprob));
-  track(p->probs_d);
-  CK(cudaMallocHost(&p->h_theta, sizeof(double) * (size_t)nprob * ldtheta));
-  CK(cudaMallocHost(&p->h_ll, sizeof(double) * nprob));
-  CK(cudaMallocHost(&p->h_info, sizeof(int) * nprob));
-  p->probs_h.resize(nprob);
-  for (int i = 0; i < nprob; ++i) {
-    Workspace ws;
-    int rc = alloc_workspace(ctxs[i], ws, &p->allocations);
-    if (rc) {
-      fgpu_plan_destroy(p.release());
-      return rc;
-    }
-    ws.status = p->status_all + 4 * i;
-    fill_prob(p->probs_h[i], ctxs[i], p->theta_d + (size_t)i * ldtheta, ws);
-    p->probs_h[i].ll_dst = p->ll_d + i;
-    p->probs_h[i].info_dst = p->info_d + i;
-  }
-  CK(cudaMemcpy(p->probs_d, p->probs_h.data(), sizeof(Prob) * nprob, cudaMemcpyHostToDevice));
   p->mode = ctxs[0]->mode;
-  if (p->mode == 1) {
-    std::vector<int> nts, tcs;
-    for (int i = 0; i < nprob; ++i) {
-      nts.push_back(ctxs[i]->nt128);
-      tcs.push_back(ctxs[i]->spec.tc_build);
+  CK(cudaSetDevice(p->device));
+  // waves under the device-memory budget
+  std::vector<size_t> bytes(nprob);
+  for (int i = 0; i < nprob; ++i) bytes[i] = workspace_bytes(ctxs[i]);
+  std::vector<std::vector<int>> groups;
+  int rc = plan_waves(bytes, plan_memory_budget(), groups);
+  if (rc) return rc;
+  for (const auto& g : groups) {
+    PlanWave w;
+    w.first = (int)p->order.size();
+    w.count = (int)g.size();
+    for (int i : g) {
+      p->order.push_back(i);
+      w.bytes += bytes[i];
+      w.max_nsteps = std::max(w.max_nsteps, ctxs[i]->nsteps);
+      w.max_nplanes = std::max(w.max_nplanes, ctxs[i]->spec.nplanes);
     }
-    int rs = build_sched(nts, tcs, p->sched, &p->allocations);
-    if (rs) {
-      fgpu_plan_destroy(p.release());
-      return rs;
-    }
+    p->arena_bytes = std::max(p->arena_bytes, w.bytes);
+    p->waves.push_back(w);
   }
-  int rc = capture(p->stream, &p->graph, p->probs_d, nprob, p->max_nsteps, p->max_nplanes, p->status_all,
-                   sizeof(int) * 4 * nprob, &p->graph_kernels, nullptr, p->mode, &p->sched);
-  if (rc) {
+  // from here on, a failure destroys the partly built plan
+  auto bail = [&](int r) {
     fgpu_plan_destroy(p.release());
-    return rc;
+    return r;
+  };
+#define PL_CK(call)                                                                            \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) {                                                                   \
+      cudaGetLastError();                                                                      \
+      return bail(fail(e_ == cudaErrorMemoryAllocation ? FGPU_ENOMEM : FGPU_ECUDA, "%s: %s", #call, \
+                       cudaGetErrorString(e_)));                                               \
+    }                                                                                          \
+  } while (0)
+  auto track_alloc = [&](void** dst, size_t n) -> cudaError_t {
+    cudaError_t e = cudaMalloc(dst, n);
+    if (e == cudaSuccess) p->allocations.push_back(*dst);
+    return e;
+  };
+  PL_CK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  PL_CK(track_alloc((void**)&p->theta_d, sizeof(double) * (size_t)nprob * ldtheta));
+  PL_CK(track_alloc((void**)&p->ll_d, sizeof(double) * nprob));
+  PL_CK(track_alloc((void**)&p->info_d, sizeof(int) * nprob));
+  PL_CK(track_alloc((void**)&p->status_all, sizeof(int) * 4 * nprob));
+  PL_CK(track_alloc((void**)&p->probs_d, sizeof(Prob) * nprob));
+  unsigned char* arena = nullptr;
+  PL_CK(track_alloc((void**)&arena, p->arena_bytes));
+  unsigned char* tmaps = nullptr;
+  if (p->mode == 1) PL_CK(track_alloc((void**)&tmaps, (size_t)512 * nprob));
+  PL_CK(cudaMallocHost(&p->h_theta, sizeof(double) * (size_t)nprob * ldtheta));
+  PL_CK(cudaMallocHost(&p->h_ll, sizeof(double) * nprob));
+  PL_CK(cudaMallocHost(&p->h_info, sizeof(int) * nprob));
+  p->probs_h.resize(nprob);
+  for (const PlanWave& w : p->waves) {
+    size_t off = 0;  // every wave starts at the arena's base
+    for (int k = w.first; k < w.first + w.count; ++k) {
+      const int i = p->order[k];
+      Workspace ws;
+      off += layout_workspace(ctxs[i], arena + off, ws);
+      ws.status = p->status_all + 4 * k;
+      if (p->mode == 1) {
+        ws.tmaps = tmaps + (size_t)512 * k;
+        if ((rc = write_tmaps(ctxs[i], ws, ws.tmaps)) != 0) return bail(rc);
+      }
+      fill_prob(p->probs_h[k], ctxs[i], p->theta_d + (size_t)i * ldtheta, ws);
+      p->probs_h[k].ll_dst = p->ll_d + i;
+      p->probs_h[k].info_dst = p->info_d + i;
+    }
   }
+  PL_CK(cudaMemcpy(p->probs_d, p->probs_h.data(), sizeof(Prob) * nprob, cudaMemcpyHostToDevice));
+  if (p->mode == 1) {
+    for (PlanWave& w : p->waves) {
+      std::vector<int> nts, tcs;
+      for (int k = w.first; k < w.first + w.count; ++k) {
+        nts.push_back(ctxs[p->order[k]]->nt128);
+        tcs.push_back(ctxs[p->order[k]]->spec.tc_build);
+      }
+      if ((rc = build_sched(nts, tcs, w.sched, &p->allocations)) != 0) return bail(rc);
+    }
+  }
+#undef PL_CK
+  if ((rc = capture_plan(p.get(), &p->graph, &p->graph_kernels, nullptr)) != 0) return bail(rc);
   *out = p.release();
   return 0;
 }
@@ -999,18 +1178,44 @@ int fgpu_plan_create(fgpu_plan** out, fgpu_ctx* const* ctxs, int nprob, int ldth
 void fgpu_plan_destroy(fgpu_plan* p) {
   if (!p) return;
   cudaSetDevice(p->device);
+  if (p->stream) cudaStreamSynchronize(p->stream);
   if (p->graph) cudaGraphExecDestroy(p->graph);
   if (p->prof) {
     p->prof->clear();
     delete p->prof;
   }
   for (void* q : p->allocations) cudaFree(q);
-  free_sched_sync(p->sched);
+  for (PlanWave& w : p->waves) free_sched_sync(w.sched);
   if (p->h_theta) cudaFreeHost(p->h_theta);
   if (p->h_ll) cudaFreeHost(p->h_ll);
   if (p->h_info) cudaFreeHost(p->h_info);
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;
+}
+
+int fgpu_plan_partition(const long long* bytes, int n, long long budget, int* wave_of, int* nwaves) {
+  t_err.clear();
+  if (!bytes || n < 1 || !wave_of || !nwaves || budget < 0) return fail(FGPU_EINVAL, "bad partition arguments");
+  std::vector<size_t> b(n);
+  for (int i = 0; i < n; ++i) {
+    if (bytes[i] < 0) return fail(FGPU_EINVAL, "bytes[%d] is negative", i);
+    b[i] = (size_t)bytes[i];
+  }
+  std::vector<std::vector<int>> groups;
+  int rc = plan_waves(b, (size_t)budget, groups);
+  if (rc) return rc;
+  for (size_t w = 0; w < groups.size(); ++w)
+    for (int i : groups[w]) wave_of[i] = (int)w;
+  *nwaves = (int)groups.size();
+  return 0;
+}
+
+int fgpu_plan_waves(const fgpu_plan* p, int* nwaves, long long* arena_bytes) {
+  t_err.clear();
+  if (!p || !nwaves || !arena_bytes) return fail(FGPU_EINVAL, "NULL argument");
+  *nwaves = (int)p->waves.size();
+  *arena_bytes = (long long)p->arena_bytes;
+  return 0;
 }
 
 int fgpu_plan_set_profiling(fgpu_plan* p, int enable) {
@@ -1031,8 +1236,7 @@ int fgpu_plan_set_profiling(fgpu_plan* p, int enable) {
   }
   cudaGraphExec_t g = nullptr;
   long long nk = 0;
-  int rc = capture(p->stream, &g, p->probs_d, p->nprob, p->max_nsteps, p->max_nplanes, p->status_all,
-                   sizeof(int) * 4 * p->nprob, &nk, p->prof, p->mode, &p->sched);
+  int rc = capture_plan(p, &g, &nk, p->prof);
   if (rc) return rc;
   if (p->graph) cudaGraphExecDestroy(p->graph);
   p->graph = g;
@@ -1108,18 +1312,35 @@ int fgpu_loglik_batch(fgpu_ctx* const* ctxs, int nprob, const double* const* the
     if (!ctxs[i] || !theta[i]) return fail(FGPU_EINVAL, "NULL entry %d", i);
     maxth = std::max(maxth, ctxs[i]->ntheta);
   }
-  fgpu_plan* p = nullptr;
+  std::shared_ptr<fgpu_plan> sp;
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     auto it = g_plans.find(key);
-    if (it != g_plans.end()) p = it->second;
+    if (it != g_plans.end()) {
+      sp = it->second.plan;
+      it->second.used = ++g_plan_clock;
+    }
   }
-  if (!p) {
-    int rc = fgpu_plan_create(&p, ctxs, nprob, std::max(maxth, 1));
+  if (!sp) {
+    fgpu_plan* raw = nullptr;
+    int rc = fgpu_plan_create(&raw, ctxs, nprob, std::max(maxth, 1));
     if (rc) return rc;
+    sp = std::shared_ptr<fgpu_plan>(raw, fgpu_plan_destroy);
+    std::vector<std::shared_ptr<fgpu_plan>> drop;  // evicted plans, destroyed outside the lock
     std::lock_guard<std::mutex> lk(g_plan_mu);
-    g_plans[key] = p;
+    CachedPlan& e = g_plans[key];
+    if (e.plan) drop.push_back(e.plan);  // another thread built the same plan meanwhile
+    e.plan = sp;
+    e.used = ++g_plan_clock;
+    while (g_plans.size() > plan_cache_limit()) {
+      auto lru = g_plans.begin();
+      for (auto it = g_plans.begin(); it != g_plans.end(); ++it)
+        if (it->second.used < lru->second.used) lru = it;
+      drop.push_back(std::move(lru->second.plan));
+      g_plans.erase(lru);
+    }
   }
+  fgpu_plan* p = sp.get();
   std::vector<double> th((size_t)nprob * p->ldtheta, 0.0);
   for (int i = 0; i < nprob; ++i) {
     for (int k = 0; k < ctxs[i]->ntheta; ++k) {

@@ -375,12 +375,8 @@ cudaError_t launch_feat_digits(const Prob* probs, int nprob, int max_nt128, cuda
 
 cudaError_t launch_build_tc(const Prob* probs, int nprob, const int* prefix, int total_tiles, int num_sms,
                             cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_build_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, BLD_SMEM);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  cudaError_t e = ensure_smem_attr((const void*)k_build_tc, SMEM_BUILD_TC, BLD_SMEM);
+  if (e != cudaSuccess) return e;
   if (total_tiles <= 0) return cudaSuccess;
   const int grid = total_tiles < num_sms ? total_tiles : num_sms;
   k_build_tc<<<grid, BLD_THREADS, BLD_SMEM, s>>>(probs, nprob, prefix);

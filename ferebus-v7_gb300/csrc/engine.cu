@@ -11,6 +11,7 @@
 #include "tc_common.cuh"
 #include "potf2_block.cuh"
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 
@@ -230,9 +231,12 @@ __global__ void __launch_bounds__(256) k_prep_planes(const Prob* __restrict__ pr
   const int l = blockIdx.y;
   if (P.mode != 1 || i >= P.Nc) return;
   const Spec& sp = *P.spec;
+  const size_t nc = (size_t)P.Nc;
+  // the workspace is not cleared between evaluations (a batch plan reuses
+  // it across problems): rows of non-rbf leaves are zeroed here
+  if (l >= sp.nleaf || sp.leaf[l].type != L_RBF) P.norms[(size_t)l * nc + i] = 0.0;
   if (l >= sp.nleaf) return;
   const Leaf& L = sp.leaf[l];
-  const size_t nc = (size_t)P.Nc;
   if (L.type == L_RBF) {
     double a = 0.0;
     for (int k = 0; k < L.n; ++k) {
@@ -641,22 +645,28 @@ __global__ void __launch_bounds__(256) k_bs_update(const Prob* __restrict__ prob
 // ---------------------------------------------------------------------------
 // launch helpers
 // ---------------------------------------------------------------------------
-static int g_build_attr_set = 0, g_update_attr_set = 0;
+static std::atomic<unsigned> g_smem_done[64];
+
+cudaError_t ensure_smem_attr(const void* func, int slot, int bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned bit = 1u << slot;
+  if (dev >= 0 && dev < 64 && (g_smem_done[dev].load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64) g_smem_done[dev].fetch_or(bit, std::memory_order_release);
+  return cudaSuccess;
+}
 
 cudaError_t launch_build(const Prob* probs, int nprob, int max_nsteps, int max_nplanes, cudaStream_t s) {
   const size_t smem = build_smem_bytes(max_nplanes);
-  if (!g_build_attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)build_smem_bytes(MAX_PLANES));
-    if (e != cudaSuccess) return e;
-    g_build_attr_set = 1;
-  }
+  cudaError_t e = ensure_smem_attr((const void*)k_build, SMEM_BUILD, (int)build_smem_bytes(MAX_PLANES));
+  if (e != cudaSuccess) return e;
   dim3 grid(max_nsteps + 1, max_nsteps, nprob);
   k_build<<<grid, 256, smem, s>>>(probs);
   return cudaGetLastError();
 }
-
-static int g_build_dot_attr_set = 0;
 
 cudaError_t launch_prep_planes(const Prob* probs, int nprob, int max_nc, cudaStream_t s) {
   k_prep_planes<<<dim3((max_nc + 255) / 256, MAX_LEAF, nprob), 256, 0, s>>>(probs);
@@ -664,12 +674,8 @@ cudaError_t launch_prep_planes(const Prob* probs, int nprob, int max_nc, cudaStr
 }
 
 cudaError_t launch_build_dot(const Prob* probs, int nprob, int max_nsteps, int max_nplanes, cudaStream_t s) {
-  if (!g_build_dot_attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_build_dot, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)build_dot_smem_bytes(MAX_PLANES));
-    if (e != cudaSuccess) return e;
-    g_build_dot_attr_set = 1;
-  }
+  cudaError_t e = ensure_smem_attr((const void*)k_build_dot, SMEM_BUILD_DOT, (int)build_dot_smem_bytes(MAX_PLANES));
+  if (e != cudaSuccess) return e;
   dim3 grid(max_nsteps + 1, max_nsteps, nprob);
   k_build_dot<<<grid, 256, build_dot_smem_bytes(max_nplanes), s>>>(probs);
   return cudaGetLastError();
@@ -702,11 +708,8 @@ cudaError_t launch_update(const Prob* probs, int nprob, int step, int max_nsteps
   const int mr = max_rowtiles - step - 1;  // trailing row tiles incl. border rows
   if (m <= 0) return cudaSuccess;
   const int smem = 2 * TB * UPD_STRIDE * (int)sizeof(double);
-  if (!g_update_attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_update, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    g_update_attr_set = 1;
-  }
+  cudaError_t e = ensure_smem_attr((const void*)k_update, SMEM_UPDATE, smem);
+  if (e != cudaSuccess) return e;
   k_update<<<dim3(mr, m, nprob), 128, smem, s>>>(probs, step);
   return cudaGetLastError();
 }

@@ -133,6 +133,17 @@ size_t build_smem_bytes(int nplanes);
 constexpr int NB = 128;
 constexpr int NSLICE = 7;                       // fp16 digit planes per FP64 value
 constexpr size_t SLICE_BYTES = 128 * 128 * 2;   // one digit plane of a 128-row x 128-k tile
+// The exact trailing sums are kept for lower-triangle tiles only (128 rows x
+// 64 columns, column-major inside): column tile tj holds row tiles
+// tj / 2 .. nt128 - 1, so a problem stores nt128 (nt128 + 1) tiles instead of
+// (2 nt128) nt128.  acc_tile is the tile's index in that packed order.
+__host__ __device__ inline size_t acc_tile(int ti, int tj, int nt128) {
+  const long long q = tj >> 1, h = tj & 1;
+  return (size_t)(2 * q * nt128 - q * (q - 1) + h * (nt128 - q) + (ti - q));
+}
+inline size_t acc_tiles(int nt128) { return (size_t)nt128 * (nt128 + 1); }
+constexpr size_t ACC_TILE_ELEMS = (size_t)NB * TB;
+
 cudaError_t launch_scales(const Prob* probs, int nprob, int max_nc, cudaStream_t s);
 cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
 // prefix: device table of nprob + 1 tile offsets for this step (tiles of
@@ -164,6 +175,17 @@ cudaError_t launch_syrk_inv(const Prob* p, int nsteps, cudaStream_t s);
 cudaError_t enqueue_grad_passes(const Prob* p, int nsteps, int nk, int optimise_noise, double* g_out,
                                 cudaStream_t s, long long* nlaunch);
 constexpr int GRAD_SLOTS = 33;  // parameters per fused pass + noise slot
+
+// Opt kernel `func` into `bytes` of dynamic shared memory on the CURRENT
+// device.  cudaFuncSetAttribute acts per device, so the record of what was
+// already set is one bit per (device, slot), updated atomically: a second
+// device, or a second thread, sets the attribute for itself.  Devices
+// beyond the first 64 set it on every call.
+enum SmemSlot {
+  SMEM_BUILD, SMEM_BUILD_DOT, SMEM_UPDATE, SMEM_SYRK, SMEM_OZAKI_UPDATE, SMEM_COUPLE1, SMEM_COUPLE2,
+  SMEM_BUILD_TC, SMEM_NSLOTS
+};
+cudaError_t ensure_smem_attr(const void* func, int slot, int bytes);
 
 // api.cu hooks for other translation units.
 int internal_compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>& plane_dim,

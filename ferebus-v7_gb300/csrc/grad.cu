@@ -247,14 +247,10 @@ cudaError_t launch_identity_border(const Prob* p, int nc, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-static bool g_syrk_attr = false;
 cudaError_t launch_syrk_inv(const Prob* p, int nsteps, cudaStream_t s) {
   const int smem = 2 * TB * USTRIDE * (int)sizeof(double);
-  if (!g_syrk_attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_syrk_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    g_syrk_attr = true;
-  }
+  cudaError_t e = ensure_smem_attr((const void*)k_syrk_inv, SMEM_SYRK, smem);
+  if (e != cudaSuccess) return e;
   k_syrk_inv<<<dim3(nsteps, nsteps), 128, smem, s>>>(p);
   return cudaGetLastError();
 }

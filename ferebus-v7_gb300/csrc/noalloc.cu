@@ -2,13 +2,13 @@
 //
 // Who needs it: hosts that may not call cudaMalloc at the moment they want a
 // likelihood -- a Fortran/OpenACC host whose device memory is owned by the
-// OpenACC runtime's data regions or by a caching pool that forbids side
-// allocations, and code that evaluates while another thread holds a
-// global-mode stream capture (cudaMalloc is then an error).  They pass device
-// pointers for the inputs and outputs; every intermediate (feature planes,
-// the kernel matrix K, log-det partials, status words, descriptors) lives in
-// one file-scope device array of fixed size, so N is limited to
-// NOALLOC_MAX_N and the feature planes to NOALLOC_MAX_PLANES.
+// OpenACC runtime's data regions, or a host whose caching pool forbids side
+// allocations.  They pass device pointers for the inputs and outputs; every
+// intermediate (feature planes, the kernel matrix K, log-det partials,
+// status words, descriptors) lives in one file-scope device array of fixed
+// size, so N is limited to NOALLOC_MAX_N and the feature planes to
+// NOALLOC_MAX_PLANES.  The descriptors travel as kernel arguments, so the
+// call enqueues its work and returns without waiting for the stream.
 //
 // The array is shared by every call in the process on that device and keeps
 // the previous call's contents; the status words are cleared at the start of
@@ -73,6 +73,18 @@ __global__ void k_noalloc_planes(const double* __restrict__ X, int N, int Nc, Pl
     v = pm.kind[p] == 1 ? sin(x / 2.0) : (pm.kind[p] == 2 ? cos(x / 2.0) : x);
   }
   planes[(size_t)p * Nc + i] = v;
+}
+
+// The call's descriptors reach the scratch as kernel arguments (no host
+// staging buffer, so the call never waits for earlier work on the stream),
+// and the status words start at zero.
+__global__ void k_noalloc_desc(Prob P, Spec sp, Prob* __restrict__ pd, Spec* __restrict__ sd,
+                               int* __restrict__ status) {
+  if (threadIdx.x == 0) {
+    *pd = P;
+    *sd = sp;
+    for (int k = 0; k < 4; ++k) status[k] = 0;
+  }
 }
 
 int scratch_address(int dev, unsigned char** out) {
@@ -166,11 +178,11 @@ extern "C" int fgpu_loglik_noalloc(int N, int d, const double* X_dev, const doub
     pm.dim[p] = plane_dim[p];
     pm.kind[p] = plane_kind[p];
   }
-  // descriptors: pageable host -> scratch (staged before the call returns)
-  NA_CK(cudaMemcpyAsync(base + OFF_SPEC, &sp, sizeof(Spec), cudaMemcpyHostToDevice, s));
-  NA_CK(cudaMemcpyAsync(base + OFF_PROB, &P, sizeof(Prob), cudaMemcpyHostToDevice, s));
-  NA_CK(cudaMemsetAsync(base + OFF_STATUS, 0, sizeof(int) * 4, s));
-  long long n = 0;
+  static_assert(sizeof(Prob) + sizeof(Spec) + 3 * sizeof(void*) <= 4000, "descriptors fit the kernel arguments");
+  k_noalloc_desc<<<1, 32, 0, s>>>(P, sp, reinterpret_cast<Prob*>(base + OFF_PROB),
+                                  reinterpret_cast<Spec*>(base + OFF_SPEC), reinterpret_cast<int*>(base + OFF_STATUS));
+  NA_CK(cudaGetLastError());
+  long long n = 1;
   if (sp.nplanes > 0) {
     k_noalloc_planes<<<dim3((Nc + 255) / 256, sp.nplanes), 256, 0, s>>>(
         X_dev, N, Nc, pm, reinterpret_cast<double*>(base + OFF_PLANES));

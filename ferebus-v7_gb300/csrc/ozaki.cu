@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
   const int ei = P.escale[i] - 62;
   for (int jj = 0; jj < 16; ++jj) {
     const int j = c0 + blockIdx.y * 16 + jj;
-    const size_t a = ((size_t)((j >> 6) * P.nt128 + (i >> 7)) * 64 + (j & 63)) * 128 + (i & 127);
+    const size_t a = (acc_tile(i >> 7, j >> 6, P.nt128) * 64 + (j & 63)) * 128 + (i & 127);
     const double w = fixed_to_double(P.acc_hi[a], P.acc_lo[a], ei + P.escale[j]);
     double* kp = P.K + (size_t)j * ld + i;
     *kp = *kp - w;
@@ -90,9 +90,10 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
 // and write them back to HBM while the tensor cores work on the next tile.
 //
 // Accumulator per element: W = hi * 2^24 + lo, hi int64, lo in [0, 2^24),
-// value = W * 2^(e_i + e_j - 62); tile-major storage (128 x 64 tiles,
-// column-major inside).  Tiles of a step are enumerated problem by problem
-// (prefix table from the host), column tile major, row tile minor.
+// value = W * 2^(e_i + e_j - 62); tile-major storage of the lower
+// triangle's 128 x 64 tiles (acc_tile), column-major inside.  Tiles of a
+// step are enumerated problem by problem (prefix table from the host),
+// column tile major, row tile minor.
 // ---------------------------------------------------------------------------
 constexpr int CH = 8;                                // k-chunks of 16 per 128-panel (one MMA each)
 constexpr int NSTAGE = 3;
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
         // chunks, so the chunk loads never wait for the epilogue); step 0
         // writes the accumulators without reading them.
         bool acc_issued = (s == 0);
-        const size_t tile = (size_t)(tj * P.nt128 + ti) * (128 * 64);
+        const size_t tile = acc_tile(ti, tj, P.nt128) * ACC_TILE_ELEMS;
         const uint32_t apar = (it & 1) ^ 1;
         for (int c = 0; c < CH; ++c, ++g) {
           if (!acc_issued && mbar_test(aempty, apar)) {
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
         hv[q] += lv[q] >> 24;
         lv[q] &= 0xFFFFFF;
       }
-      const size_t tile = (size_t)(tj * P.nt128 + ti) * (128 * 64);
+      const size_t tile = acc_tile(ti, tj, P.nt128) * ACC_TILE_ELEMS;
       long long* gh = P.acc_hi + tile;
       int* gl = P.acc_lo + tile;
       const bool first = (s == 0);
@@ -931,21 +932,11 @@ int encode_slice_maps(void* host_maps, const void* slices, int nt128) {
 // ---------------------------------------------------------------------------
 // launch helpers
 // ---------------------------------------------------------------------------
-static bool g_attr = false;
 static cudaError_t set_attrs() {
-  if (g_attr) return cudaSuccess;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_ozaki_update, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM)) !=
-      cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_couple<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, CPL_SMEM)) !=
-      cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_couple<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, CPL_SMEM)) !=
-      cudaSuccess)
-    return e;
-  g_attr = true;
-  return cudaSuccess;
+  if ((e = ensure_smem_attr((const void*)k_ozaki_update, SMEM_OZAKI_UPDATE, UPD_SMEM)) != cudaSuccess) return e;
+  if ((e = ensure_smem_attr((const void*)k_couple<1>, SMEM_COUPLE1, CPL_SMEM)) != cudaSuccess) return e;
+  return ensure_smem_attr((const void*)k_couple<2>, SMEM_COUPLE2, CPL_SMEM);
 }
 
 cudaError_t launch_scales(const Prob* probs, int nprob, int max_nc, cudaStream_t s) {

@@ -19,7 +19,7 @@ EXPORTS = (
     "fgpu_plan_create", "fgpu_plan_run_device", "fgpu_plan_run", "fgpu_plan_destroy",
     "fgpu_destroy", "fgpu_last_error", "fgpu_version", "fgpu_last_launch_count",
     "fgpu_plan_set_profiling", "fgpu_plan_stage_times", "fgpu_loglik_noalloc",
-    "fgpu_set_trailing_update", "fgpu_diag_exp",
+    "fgpu_set_trailing_update", "fgpu_diag_exp", "fgpu_plan_waves", "fgpu_plan_partition",
 )
 
 c_double_p = C.POINTER(C.c_double)
@@ -82,6 +82,10 @@ def load(path=None):
     lib.fgpu_set_trailing_update.restype = C.c_int
     lib.fgpu_diag_exp.argtypes = [c_double_p, c_double_p, C.c_int]
     lib.fgpu_diag_exp.restype = C.c_int
+    lib.fgpu_plan_waves.argtypes = [vp, c_int_p, C.POINTER(C.c_longlong)]
+    lib.fgpu_plan_waves.restype = C.c_int
+    lib.fgpu_plan_partition.argtypes = [C.POINTER(C.c_longlong), C.c_int, C.c_longlong, c_int_p, c_int_p]
+    lib.fgpu_plan_partition.restype = C.c_int
     _lib = lib
     return lib
 

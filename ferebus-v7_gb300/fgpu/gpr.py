@@ -120,6 +120,12 @@ class Plan:
     def launches(self):
         return int(self.lib.fgpu_last_launch_count())
 
+    def waves(self):
+        """(number of waves, bytes of the shared workspace arena)."""
+        nw, ab = C.c_int(), C.c_longlong()
+        _lib.check(self.lib.fgpu_plan_waves(self.handle, C.byref(nw), C.byref(ab)))
+        return nw.value, ab.value
+
     def set_profiling(self, enable=True):
         """True: event nodes around every launch; "update": around the
         trailing-update launches only; False: off."""
@@ -155,6 +161,19 @@ def set_trailing_update(mode):
     code = {"fp64": 0, "tcgen05": 1}[mode]
     prev = _lib.check(lib.fgpu_set_trailing_update(code))
     return {0: "fp64", 1: "tcgen05"}[prev]
+
+
+def plan_partition(nbytes, budget):
+    """The wave partition a plan applies to problems with these workspace
+    sizes under ``budget`` bytes (host-only): returns (wave of each problem,
+    number of waves)."""
+    lib = _lib.load()
+    n = len(nbytes)
+    b = (C.c_longlong * n)(*[int(v) for v in nbytes])
+    w = (C.c_int * n)()
+    nw = C.c_int()
+    _lib.check(lib.fgpu_plan_partition(b, n, int(budget), w, C.byref(nw)))
+    return list(w), nw.value
 
 
 def loglik_batch(engines, thetas):

@@ -21,6 +21,23 @@ The forced swarm updater (pso.f90:485-558) updates the global best inside the
 particle loop, so its trajectory is inherently sequential; it is not offered
 here.  Random numbers come from numpy's PCG64, not the reference's RNG, so
 trajectories match the reference in distribution, not bit for bit.
+
+Gradient polish (``SwarmConfig.polish_steps > 0``; off by default, and then
+nothing below runs): after the last iteration each swarm's global best is
+refined by projected gradient ascent on logL with the engine's FP64 adjoint
+(``fgpu_grad``), in box-normalised coordinates u = (theta - lo) / (hi - lo)
+so that the linear noise parameter (box [1e-12, 1e-6]) and the kernel
+parameters move on the same scale.  Each step tries a move of at most
+``polish_move`` of the box along the gradient, halves it until logL improves
+(at most ``polish_halvings`` times) and keeps only improving moves, so the
+polished cost is never above the swarm's.  Moves are projected onto the
+search box widened to contain the starting point: the reference's swarm has
+no search boundaries (pso.f90:431, "TODO: Implement search boundaries") and
+its global best may lie outside the box, and the polish goes no further out.  The reference has no gradient
+(negative_log_likelihood, src/model/gpr/gpr.f90:258-289, ignores its
+``gradient`` flag); the polish starts from the global best the reference's
+serial update keeps (pso.f90:454-459) and leaves the swarm's trajectory
+untouched.
 """
 from __future__ import annotations
 
@@ -42,6 +59,9 @@ class SwarmConfig:
     stall_iterations: int = 0        # 0: no relative-change stopping
     tolerance: float = 1e-8
     max_retries: int = 64            # bound on re-randomisations per particle per iteration
+    polish_steps: int = 0            # gradient-polish steps of each global best (0: off)
+    polish_move: float = 0.05        # largest first move per step, as a fraction of the box
+    polish_halvings: int = 10
 
 
 @dataclass
@@ -188,4 +208,47 @@ class LockstepPSO:
         for _ in range(iterations if iterations is not None else self.cfg.iterations):
             if self.step():
                 break
+        if self.cfg.polish_steps > 0:
+            self.polish()
         return [(st.gbest_x, st.gbest_cost) for st in self.states]
+
+    def polish(self, steps=None):
+        """Projected gradient ascent on logL from each swarm's global best
+        (see the module docstring); updates gbest_x / gbest_cost only where
+        logL improves.  Returns per swarm the list of accepted costs."""
+        steps = self.cfg.polish_steps if steps is None else steps
+        out = []
+        for a, st in enumerate(self.states):
+            eng = self.engines[a]
+            x, cost = st.gbest_x.copy(), st.gbest_cost
+            width = np.where(st.hi > st.lo, st.hi - st.lo, 1.0)
+            lo, hi = np.minimum(st.lo, x), np.maximum(st.hi, x)
+            accepted = []
+            if not np.isfinite(cost):
+                out.append(accepted)
+                continue
+            for _ in range(steps):
+                ll, g, info = eng.grad(x)
+                if info != 0 or not np.all(np.isfinite(g)):
+                    break
+                gu = g * width                      # d logL / du
+                norm = float(np.max(np.abs(gu)))
+                if norm == 0.0:
+                    break
+                t = self.cfg.polish_move / norm
+                moved = False
+                for _h in range(self.cfg.polish_halvings + 1):
+                    xn = np.clip(x + t * gu * width, lo, hi)
+                    lln, infon = eng.loglik(xn)
+                    if infon == 0 and np.isfinite(lln) and -lln < cost:
+                        x, cost, moved = xn, -lln, True
+                        break
+                    t *= 0.5
+                if not moved:
+                    break
+                accepted.append(cost)
+            st.gbest_x, st.gbest_cost = x, cost
+            st.history.append(cost)
+            out.append(accepted)
+        self.polish_accepted = out
+        return out

@@ -114,7 +114,16 @@ int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll,
 /* Device-resident batch plan (inputs and outputs stay in HBM).  theta_dev is
  * nprob x ldtheta doubles on the device; ll_dev / info_dev are device arrays of
  * nprob entries.  stream is a cudaStream_t (NULL = the plan's own stream).
- * Used by the throughput benchmark and by hosts that keep the swarm on the GPU. */
+ * Used by the throughput benchmark and by hosts that keep the swarm on the GPU.
+ * A plan whose problems' workspaces exceed the device-memory budget (the
+ * free memory less a reserve, or FGPU_PLAN_MEM_BUDGET_MB) runs them in waves
+ * that share one workspace arena, still as one graph replay per run; a single
+ * problem larger than the budget is FGPU_ENOMEM.  After fgpu_plan_run_device,
+ * info_dev[p] < 0 means -1: a bounded device wait gave up (fgpu_plan_run
+ * returns FGPU_ETIMEOUT for it), -2: a panel value broke its row-scale bound
+ * (fgpu_plan_run returns FGPU_ECUDA); ll_dev[p] is then NaN.  No counterpart
+ * in the reference (its particles are evaluated one per OpenMP thread,
+ * src/optimiser/pso/pso.f90:419-452). */
 int fgpu_plan_create(fgpu_plan** plan, fgpu_ctx* const* ctxs, int nprob, int ldtheta);
 int fgpu_plan_run_device(fgpu_plan* plan, const double* theta_dev, double* ll_dev,
                          int* info_dev, void* stream);
@@ -122,24 +131,38 @@ int fgpu_plan_run(fgpu_plan* plan, const double* theta_host, double* ll_host,
                   int* info_host);
 void fgpu_plan_destroy(fgpu_plan* plan);
 
+/* The waves a plan runs in and the bytes of its shared workspace arena. */
+int fgpu_plan_waves(const fgpu_plan* plan, int* nwaves, long long* arena_bytes);
+
+/* Host-only: the wave partition fgpu_plan_create applies to problems of
+ * the given workspace sizes under `budget` bytes (wave_of[i] receives
+ * problem i's wave).  Touches no device; for checking the partition rule. */
+int fgpu_plan_partition(const long long* bytes, int n, long long budget, int* wave_of, int* nwaves);
+
 void fgpu_destroy(fgpu_ctx* ctx);
 
 /* One evaluation that allocates no device memory.  No counterpart in the
  * reference: it exists for hosts that may not call cudaMalloc when they need
- * a likelihood (device memory owned by an OpenACC runtime's data regions or
- * by a pool that forbids side allocations; a thread evaluating while a
- * global-mode stream capture is active elsewhere in the process).  Inputs
- * (X(N,d) column-major, y, mu, theta) and outputs (ll, info: one value each)
- * are DEVICE pointers; kspec is host memory.  All intermediates live in one
- * fixed static device array (about 9.5 MB per device, held until the process
+ * a likelihood (device memory owned by an OpenACC runtime's data regions, or
+ * by a pool that forbids side allocations).  Inputs (X(N,d) column-major, y,
+ * mu, theta: theta holds the kernel parameters and, with optimise_noise, the
+ * linear noise value last) and outputs (ll, info: one value each) are DEVICE
+ * pointers; kspec is host memory.  All intermediates live in one fixed
+ * static device array (about 9.5 MB per device, held until the process
  * exits), so N <= FGPU_NOALLOC_MAX_N and the kernel spec may need at most
  * FGPU_NOALLOC_MAX_PLANES feature planes (one per rbf dim, two per periodic
- * dim); larger inputs are rejected with FGPU_EINVAL.  The work is enqueued on
- * `stream` (a cudaStream_t, NULL = legacy default) and the call returns
- * without waiting.  The first call on a device resolves the array's address
+ * dim); larger inputs are rejected with FGPU_EINVAL before any device work.
+ * The work, including the copy of the call's descriptors (passed as kernel
+ * arguments, no host staging buffer), is enqueued on `stream` (a
+ * cudaStream_t, NULL = legacy default) and the call returns without waiting
+ * for it; read ll/info after synchronising with the stream.  *info_dev is 0,
+ * a LAPACK-style pivot column > 0 (non-positive-definite K, ll NaN), or
+ * negative: -1 a bounded device wait gave up (what other entry points report
+ * as FGPU_ETIMEOUT), -2 a panel value broke its row-scale bound (FGPU_ECUDA).
+ * The first call on a device resolves the array's address
  * (cudaGetSymbolAddress) -- make it before any stream capture.  Every call
- * shares the array: calls that overlap on the GPU race and must be
- * serialised by the caller. */
+ * shares the array and finds the previous call's contents there: calls
+ * that overlap on the GPU race and must be serialised by the caller. */
 #define FGPU_NOALLOC_MAX_N 1024
 #define FGPU_NOALLOC_MAX_PLANES 64
 int fgpu_loglik_noalloc(int N, int d, const double* X_dev, const double* y_dev, const double* mu_dev,

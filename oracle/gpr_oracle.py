@@ -213,15 +213,25 @@ def leaf_R(op, dims, params, tens: Tensors):
     if tens.lazy and op in (RBF, PERIODIC, RBF_CYCLIC):
         if op == RBF_CYCLIC and len(dims) != d:
             raise ValueError("rbf-cyclic requires active_dims == all features (reference shape rule)")
+        # blocks of columns j0..j1-1, rows j0..n-1, with the same arithmetic as
+        # the stored tensors: diff*diff, sin(sqrt(D)/2)**2, l . D over the
+        # dims (a dgemv in the reference), exp
         R = np.zeros((n, n))
-        for j in range(n):
-            D, P, Cc = tens.column(j)
-            if op == RBF:
-                R[j:, j] = np.exp(-0.5 * (params @ D[dims]))
-            elif op == PERIODIC:
-                R[j:, j] = np.exp(-2.0 * (params @ P[dims]))
+        B = max(1, int(4e6 // (n * max(len(dims), 1))))
+        for j0 in range(0, n, B):
+            j1 = min(n, j0 + B)
+            diff = X[j0:, None, dims] - X[None, j0:j1, dims]        # (n - j0, b, k)
+            if op == RBF_CYCLIC:
+                cyc = [q for q, dm in enumerate(dims) if dm % 3 == 2]
+                c = diff[:, :, cyc]
+                a = np.abs(c) + PI
+                diff[:, :, cyc] = np.where(c == 0.0, 0.0, np.sign(c) * ((a - np.trunc(a / TWOPI) * TWOPI) - PI))
+            D = diff * diff
+            if op == PERIODIC:
+                P = np.sin(np.sqrt(D) / 2.0)
+                R[j0:, j0:j1] = np.exp(-2.0 * ((P * P) @ params))
             else:
-                R[j:, j] = np.exp(-0.5 * (params @ Cc))
+                R[j0:, j0:j1] = np.exp(-0.5 * (D @ params))
         return R
     if op == RBF:
         return np.exp(_gemv_t(tens.D, dims, params, -0.5))

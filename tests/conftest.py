@@ -40,3 +40,24 @@ def lib():
     if not os.path.exists(build.LIB_PATH):
         build.build_library()
     return _lib.load()
+
+
+def parity_tol(ll_exact, ll_openblas, fp64_err):
+    """Bound on |ll_engine - ll_exact| for one parameter vector.
+
+    ``ll_exact`` is the likelihood evaluated in extended precision
+    (oracle/exact.py), ``ll_openblas`` the oracle's FP64 value through
+    OpenBLAS dpotrf/dpotrs (the reference's LAPACK path), ``fp64_err`` the FP64
+    error scale: the largest distance to ``ll_exact`` over OpenBLAS, MKL and
+    OpenBLAS on eight 4-ulp perturbations of K.
+
+    * The engine may be no further from the exact value than twice the worst
+      of those FP64 evaluations (with a floor of 1e-11 |ll| for well
+      conditioned K, where every FP64 evaluation is within a few ulp);
+    * wherever OpenBLAS itself is within 1e-9 |ll| of the exact value, the
+      engine must be too (the 1e-9 relative target).
+    """
+    t = max(2.0 * fp64_err, 1e-11 * abs(ll_exact))
+    if abs(ll_openblas - ll_exact) <= 1e-9 * abs(ll_exact):
+        t = min(t, 1e-9 * abs(ll_exact))
+    return t

@@ -1,16 +1,30 @@
 """Generate the golden fixtures under tests/golden/ from the CPU oracle.
 
 Run in the development container (it reads the reference's example CSVs,
-which do not travel to the GPU machine):
+which do not travel to the GPU machine); ``--examples-dir`` is the
+``examples`` folder of a FEREBUS-v7 checkout:
 
-    python tests/golden/make_golden.py [--examples-dir DIR]
+    python tests/golden/make_golden.py --examples-dir <FEREBUS-v7>/examples
 
 Each ``<case>.npz`` holds the inputs (X, y, mu, kspec, likelihood, noise,
-optimise_noise), a few parameter vectors, and the oracle's outputs for each:
-ll, info, logdet and -- for the first vector -- alpha.  ``spread`` is the
-case's FP64 noise floor: the largest |ll' - ll| over an independent LAPACK
-(MKL cholesky/cholesky_solve) and three random 4-ulp symmetric perturbations
-of K; tests set their tolerance to max(1e-9 |ll|, 4 * spread).
+optimise_noise), a few parameter vectors, and for each of them:
+
+* ``ll`` -- the oracle's value (OpenBLAS dpotrf/dpotrs, the reference's LAPACK
+  path), with ``info`` and ``logdet``, and ``alpha0`` for the first vector;
+* ``ll_exact`` -- the same formulas in extended precision
+  (``oracle/exact.py``, 64-bit significand on x86-64), the value FP64 codes
+  are measured against;
+* ``fp64_err`` -- the FP64 error scale: the largest |ll' - ll_exact| over
+  OpenBLAS, an independent LAPACK (MKL through torch) and OpenBLAS on eight
+  random symmetric 4-ulp perturbations of K (the backward error any FP64
+  evaluation of K and its Cholesky carries);
+* ``spread`` -- the largest |ll' - ll| over MKL and three such perturbations
+  (kept for reference).
+
+``full_size.json`` holds the same quantities for the two ill-conditioned
+benchmark shapes at their full size (water-like N=500, methanol-like
+N=2000), with their targets y; the tests regenerate the features X from the
+seeded generators and check them against the stored SHA-256 digest.
 
 Example data (examples/*/..._TRAINING_SET.csv of FEREBUS-v7) are stored as
 row subsets of the feature columns and the ``iqa`` target only.
@@ -30,6 +44,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "ferebus-v7_gb300"))
 
 from oracle import gpr_oracle as O  # noqa: E402
+from oracle import exact as E  # noqa: E402
 from fgpu import synth  # noqa: E402
 from fgpu.kernel_spec import build_kspec  # noqa: E402
 
@@ -104,6 +119,21 @@ def noise_floor(K, y, mu, likelihood, ll, rng, trials=3):
     return worst
 
 
+def fp64_error_scale(K, y, mu, likelihood, ll_ob, ll_exact, rng, trials=8):
+    """Largest |ll' - ll_exact| over OpenBLAS, MKL and OpenBLAS on `trials`
+    random symmetric perturbations K_ij (1 + e_ij), |e_ij| <= 4 u."""
+    u = np.finfo(np.float64).eps / 2
+    worst = max(abs(ll_ob - ll_exact), abs(mkl_ll(K, y, mu, likelihood) - ll_exact))
+    Ks = np.tril(K) + np.tril(K, -1).T
+    for _ in range(trials):
+        Ep = rng.uniform(-4 * u, 4 * u, size=K.shape)
+        Ep = np.tril(Ep) + np.tril(Ep, -1).T
+        lp = ll_from_K(Ks * (1.0 + Ep), y, mu, likelihood)
+        if np.isfinite(lp):
+            worst = max(worst, abs(lp - ll_exact))
+    return worst
+
+
 def make_case(name, X, y, mean, kspec, likelihood, noise=1e-10, optimise_noise=False, thetas=None,
               seed=0, lo=1e-3, hi=1.0):
     rng = np.random.default_rng(seed)
@@ -114,7 +144,7 @@ def make_case(name, X, y, mean, kspec, likelihood, noise=1e-10, optimise_noise=F
         if optimise_noise:
             thetas[:, nk] = 10.0 ** rng.uniform(-12, -6, size=4)
     tens = O.Tensors(X, need_cyclic=O.RBF_CYCLIC in kspec)
-    out = {k: [] for k in ("ll", "info", "logdet", "spread")}
+    out = {k: [] for k in ("ll", "info", "logdet", "spread", "ll_exact", "fp64_err")}
     alpha0 = None
     for t, th in enumerate(thetas):
         r = O.loglik(kspec, th, X, y, mu, likelihood, noise, optimise_noise, tens=tens, want=True)
@@ -125,23 +155,64 @@ def make_case(name, X, y, mean, kspec, likelihood, noise=1e-10, optimise_noise=F
             nz = float(th[nk]) if optimise_noise else noise
             K = O.compute_R(kspec, th[:nk], nz, tens)
             out["spread"].append(noise_floor(K, y, mu, likelihood, r["ll"], rng))
+            ex = E.loglik_ld(kspec, th, X, y, mu, likelihood, noise, optimise_noise)[0]
+            out["ll_exact"].append(ex)
+            out["fp64_err"].append(fp64_error_scale(K, y, mu, likelihood, r["ll"], ex, rng))
         else:
             out["spread"].append(0.0)
+            out["ll_exact"].append(float("nan"))
+            out["fp64_err"].append(0.0)
         if t == 0:
             alpha0 = r["alpha"] if r["alpha"] is not None else np.zeros(len(y))
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, X=X, y=y, mu=mu, kspec=np.array(kspec, dtype=np.int32), likelihood=likelihood,
                         noise=noise, optimise_noise=int(optimise_noise), thetas=np.array(thetas),
                         ll=np.array(out["ll"]), info=np.array(out["info"], dtype=np.int32),
-                        logdet=np.array(out["logdet"]), spread=np.array(out["spread"]), alpha0=alpha0)
-    print(f"{name:24s} N={len(y):5d} d={X.shape[1]:3d} ll={out['ll']} info={out['info']} "
-          f"rel_spread={[s / max(abs(l), 1e-300) for s, l in zip(out['spread'], out['ll'])]}")
+                        logdet=np.array(out["logdet"]), spread=np.array(out["spread"]), alpha0=alpha0,
+                        ll_exact=np.array(out["ll_exact"]), fp64_err=np.array(out["fp64_err"]))
+    print(f"{name:24s} N={len(y):5d} d={X.shape[1]:3d} info={out['info']} rel_fp64_err="
+          f"{['%.1e' % (s / max(abs(l), 1e-300)) for s, l in zip(out['fp64_err'], out['ll_exact'])]}")
+
+
+def digest(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def make_full_size():
+    """full_size.json: the ill-conditioned benchmark shapes at full size."""
+    import json
+    res = {}
+    for key, p in (("water_like_500", synth.config1()), ("methanol_like_2000", synth.config2())):
+        rng = np.random.default_rng(31)
+        mu = O.mean_vector(p.mean, p.X, p.y)
+        th = p.thetas(3, seed=5)
+        tens = O.Tensors(p.X, lazy=True)
+        nk = O.kernel_nparams(p.kspec)
+        rows = []
+        for t in th:
+            K = O.compute_R(p.kspec, t[:nk], p.noise, tens)
+            ob = ll_from_K(K, p.y, mu, p.likelihood)
+            ex = E.loglik_ld(p.kspec, t, p.X, p.y, mu, p.likelihood, p.noise, False)[0]
+            err = fp64_error_scale(K, p.y, mu, p.likelihood, ob, ex, rng)
+            rows.append({"theta": [float(v) for v in t], "ll_openblas": ob, "ll_exact": ex, "fp64_err": err})
+            print(f"{key} rel_fp64_err={err / abs(ex):.2e} rel_openblas_err={abs(ob - ex) / abs(ex):.2e}")
+        # y is stored: the generator forms it through a BLAS product, whose
+        # last bits differ between machines; X is regenerated and checked
+        res[key] = {"N": p.N, "d": p.d, "X_sha256": digest(p.X), "y": [float(v) for v in p.y], "mean": p.mean,
+                    "thetas": rows}
+    with open(os.path.join(HERE, "full_size.json"), "w") as f:
+        json.dump(res, f, indent=1)
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--examples-dir", default="/root/reference/examples")
+    ap.add_argument("--examples-dir", required=True, help="the examples folder of a FEREBUS-v7 checkout")
+    ap.add_argument("--full-size-only", action="store_true")
     a = ap.parse_args()
+    make_full_size()
+    if a.full_size_only:
+        return
     ex = a.examples_dir
     R = O.RBF
     # --- the reference's shipped example data sets ---------------------------------

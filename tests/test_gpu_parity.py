@@ -1,11 +1,15 @@
 """GPU parity: the CUDA engine (through the C-ABI) against the CPU oracle.
 
-Tolerance on the log-likelihood: max(1e-9 * |ll|, 4 * spread), where
-``spread`` is the case's measured LAPACK-to-LAPACK difference (OpenBLAS
-dpotrf/dpotrs vs MKL) for the same K.  Where K is well conditioned the
-spread is ~1e-15 relative and the bar is the 1e-9 relative target; for the
-ill-conditioned water-like sets (nugget 1e-10, cond(K) ~ 1e12) no two LAPACKs
-agree to 1e-9 and the bar is their own disagreement.
+Log-likelihoods of the golden cases are measured against their
+extended-precision value (``ll_exact``, oracle/exact.py) with the rule of
+conftest.parity_tol: no further from it than twice the worst of ten FP64
+evaluations of the same likelihood (OpenBLAS, MKL, OpenBLAS on eight 4-ulp
+perturbations of K), and within 1e-9 |ll| wherever OpenBLAS itself is.  Where
+K is well conditioned every FP64 evaluation is within ~1e-15 of the exact
+value and the bar is the 1e-9 target; for the water-like sets (nugget 1e-10,
+cond(K) ~ 1e12) no FP64 evaluation is within 1e-9 and the bar is the FP64
+error scale.  Randomly generated problems (well conditioned, nugget 1e-6)
+are compared with the OpenBLAS oracle at 1e-9 relative.
 """
 import math
 import threading
@@ -13,14 +17,14 @@ import threading
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_case
+from conftest import golden_cases, load_case, parity_tol
 from oracle import gpr_oracle as O
 
 pytestmark = pytest.mark.gpu
 
 
-def tol(ll, spread):
-    return max(1e-9 * abs(ll), 4.0 * spread)
+def tol(c, k):
+    return parity_tol(float(c["ll_exact"][k]), float(c["ll"][k]), float(c["fp64_err"][k]))
 
 
 def engine_for(c):
@@ -40,7 +44,7 @@ def test_golden_loglik(name, lib):
             assert info >= c["info"][k] - 1
         else:
             assert info == 0, (k, info)
-            assert abs(ll - c["ll"][k]) <= tol(c["ll"][k], c["spread"][k]), (k, ll, c["ll"][k])
+            assert abs(ll - c["ll_exact"][k]) <= tol(c, k), (k, ll, c["ll_exact"][k], c["ll"][k])
 
 
 @pytest.mark.parametrize("name", [n for n in golden_cases() if "not_pd" not in n])
@@ -64,7 +68,7 @@ def test_golden_alpha_is_a_backward_stable_solve(name, lib):
         r = c["y"] - res["mean"]
     resid = np.linalg.norm(K @ alpha - r)
     assert resid <= 1e-12 * np.linalg.norm(K, 2) * np.linalg.norm(alpha) + 1e-14 * np.linalg.norm(r)
-    if c["spread"][0] <= 1e-12 * abs(c["ll"][0]):
+    if c["fp64_err"][0] <= 1e-12 * abs(c["ll_exact"][0]):
         ref = c["alpha0"]
         assert np.linalg.norm(alpha - ref) <= 1e-7 * np.linalg.norm(ref)
 
@@ -223,4 +227,4 @@ def test_golden_cases_in_both_modes(name, trailing):
     for k, th in enumerate(c["thetas"]):
         ll, info = e.loglik(th)
         assert info == int(c["info"][k]) == 0
-        assert abs(ll - c["ll"][k]) <= tol(c["ll"][k], c["spread"][k]), (trailing, k, ll, c["ll"][k])
+        assert abs(ll - c["ll_exact"][k]) <= tol(c, k), (trailing, k, ll, c["ll_exact"][k])

@@ -74,3 +74,61 @@ def test_relative_change_stopping():
         steps += 1
         assert steps < 500
     assert all(st.stall_count >= 3 for st in pso.states)
+
+
+class FakeEngine:
+    """logL = -sum (x - centre)^2 with its exact gradient (the engine's
+    loglik / grad interface)."""
+
+    def __init__(self, centre):
+        self.centre = np.asarray(centre, float)
+        self.grads = 0
+
+    def loglik(self, x):
+        return -float(np.sum((np.asarray(x) - self.centre) ** 2)), 0
+
+    def grad(self, x):
+        self.grads += 1
+        x = np.asarray(x, float)
+        return -float(np.sum((x - self.centre) ** 2)), -2.0 * (x - self.centre), 0
+
+
+def make_polish(centres, steps, S=6, iterations=3):
+    boxes = [(np.zeros(len(c)), np.ones(len(c))) for c in centres]
+    cfg = SwarmConfig(swarm_size=S, iterations=iterations, polish_steps=steps)
+    owner = np.repeat(np.arange(len(centres)), S)
+    fake = FakeBatch([np.asarray(c, float) for c in centres], owner)
+    engines = [FakeEngine(c) for c in centres]
+    return LockstepPSO([(e, lo, hi) for e, (lo, hi) in zip(engines, boxes)], cfg, seed=5, evaluate=fake), engines
+
+
+def test_polish_off_leaves_the_trajectory_alone_and_on_only_improves():
+    centres = [[0.31, 0.62], [0.2, 0.9, 0.45]]
+    plain, e0 = make_polish(centres, steps=0)
+    best0 = plain.run()
+    assert all(e.grads == 0 for e in e0)          # off: the adjoint is never called
+    polished, e1 = make_polish(centres, steps=20)
+    best1 = polished.run()
+    for s0, s1 in zip(plain.states, polished.states):
+        n = len(s0.history)
+        assert s1.history[:n] == s0.history        # the swarm's own trajectory is bit-identical
+        assert s1.gbest_cost <= s0.gbest_cost
+    for (x, cost), c in zip(best1, centres):
+        assert cost < 1e-6 and np.allclose(x, c, atol=1e-3)
+    assert all(e.grads > 0 for e in e1)
+
+
+def test_polish_projects_onto_the_box_widened_to_its_start():
+    # optimum outside the unit box: the polish ends on the face of the box
+    # (widened to contain the swarm's global best, which may be outside it:
+    # the reference's swarm has no boundaries), never beyond it
+    pso, _ = make_polish([[1.4, 0.5]], steps=40, iterations=2)
+    pso.initialise()
+    for _ in range(2):
+        pso.step()
+    x0 = pso.states[0].gbest_x.copy()
+    pso.polish()
+    x = pso.states[0].gbest_x
+    lo, hi = np.minimum(0.0, x0), np.maximum(1.0, x0)
+    assert np.all(x >= lo - 1e-15) and np.all(x <= hi + 1e-15)
+    assert abs(x[0] - min(1.4, hi[0])) < 1e-3 and abs(x[1] - 0.5) < 1e-3

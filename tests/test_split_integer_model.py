@@ -4,7 +4,8 @@
 arithmetic in numpy (55-bit digits in per-row scales, the digit-product
 levels kept, exact integer accumulation across panels, one rounding per
 element).  With the engine's 7 levels every golden case's log-likelihood
-meets the parity tolerance against the oracle's LAPACK value; with fewer
+meets the parity tolerance (conftest.parity_tol, against the
+extended-precision value); with fewer
 levels some do not, which shows that the test can fail and that 7 is the
 smallest level count the fixtures accept (measured: 6 levels miss the
 ammonia set by ~2400x its tolerance, 5 levels by ~4e4x).  A second model
@@ -15,13 +16,14 @@ import numpy as np
 import pytest
 
 import split_integer_model as M
-from conftest import golden_cases, load_case
+from conftest import golden_cases, load_case, parity_tol
 from oracle import gpr_oracle as O
 
 
 def _worst_ratio(name, levels, quarters=False):
-    """max over the case's PD thetas of |ll_model - ll_oracle| / tolerance;
-    `quarters`: the panel worked in the engine's quarters and halves."""
+    """max over the case's PD thetas of |ll_model - ll_exact| / tolerance
+    (conftest.parity_tol); `quarters`: the panel worked in the engine's
+    quarters and halves."""
     c = load_case(name)
     ks = [int(v) for v in c["kspec"]]
     nk = O.kernel_nparams(ks)
@@ -36,8 +38,8 @@ def _worst_ratio(name, levels, quarters=False):
         if info != 0:
             return np.inf, compared
         ll = M.loglik_from_factor(L, c["y"], c["mu"], int(c["likelihood"]))
-        tol = max(1e-9 * abs(c["ll"][k]), 4.0 * c["spread"][k])
-        worst = max(worst, abs(ll - c["ll"][k]) / tol)
+        tol = parity_tol(c["ll_exact"][k], c["ll"][k], c["fp64_err"][k])
+        worst = max(worst, abs(ll - c["ll_exact"][k]) / tol)
         compared += 1
     return worst, compared
 

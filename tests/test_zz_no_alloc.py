@@ -28,7 +28,7 @@ def _problem(n, d, seed):
     return X, y, mu, ks
 
 
-def _call_noalloc(lib, torch, X, y, mu, ks, lik, noise, theta, stream):
+def _call_noalloc(lib, torch, X, y, mu, ks, lik, noise, optimise_noise, theta, stream):
     n, d = X.shape
     Xd = torch.tensor(np.asfortranarray(X).ravel(order="F"), dtype=torch.float64, device="cuda")
     yd = torch.tensor(y, dtype=torch.float64, device="cuda")
@@ -38,7 +38,7 @@ def _call_noalloc(lib, torch, X, y, mu, ks, lik, noise, theta, stream):
     infod = torch.full((1,), -7, dtype=torch.int32, device="cuda")
     ksa = (C.c_int * len(ks))(*ks)
     rc = lib.fgpu_loglik_noalloc(n, d, C.c_void_p(Xd.data_ptr()), C.c_void_p(yd.data_ptr()),
-                                 C.c_void_p(mud.data_ptr()), ksa, len(ks), lik, noise, 0,
+                                 C.c_void_p(mud.data_ptr()), ksa, len(ks), lik, noise, int(optimise_noise),
                                  C.c_void_p(thd.data_ptr()), C.c_void_p(lld.data_ptr()),
                                  C.c_void_p(infod.data_ptr()), C.c_void_p(stream.cuda_stream))
     assert rc == 0, lib.fgpu_last_error()
@@ -47,21 +47,36 @@ def _call_noalloc(lib, torch, X, y, mu, ks, lik, noise, theta, stream):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 63, 65, 300, NOALLOC_MAX_N])
 @pytest.mark.parametrize("lik", [0, 1])
-def test_noalloc_matches_the_context_entry_point_on_two_calls(lik, lib):
+@pytest.mark.parametrize("optimise_noise", [False, True])
+def test_noalloc_matches_the_context_entry_point_on_two_calls(n, lik, optimise_noise, lib):
+    """Sizes from one point up to the scratch limit, where K, the log-det
+    parts and the solve vector fill their fixed slots exactly; with the noise
+    as the last parameter when it is optimised."""
     torch = pytest.importorskip("torch")
     from fgpu import Engine
-    X, y, mu, ks = _problem(300, 5, seed=40 + lik)
+    X, y, mu, ks = _problem(n, 5, seed=40 + lik + 7 * n)
     noise = 1e-6
-    eng = Engine(X, y, mu, ks, lik, noise, False)
-    rng = np.random.default_rng(3)
+    eng = Engine(X, y, mu, ks, lik, noise, optimise_noise)
+    rng = np.random.default_rng(3 + n)
     stream = torch.cuda.Stream()
     for call in range(2):   # the second call reuses the static scratch left by the first
         th = rng.uniform(0.0, 1.0, size=eng.ntheta)
+        if optimise_noise:
+            # read from theta, not the fixed noise: a value the context's
+            # 1e-6 cannot stand in for, kept large enough that K is well
+            # conditioned (the two paths round differently)
+            th[-1] = rng.uniform(3e-6, 3e-5)
         want, winfo = eng.loglik(th)
-        got, ginfo = _call_noalloc(lib, torch, X, y, mu, ks, lik, noise, th, stream)
+        got, ginfo = _call_noalloc(lib, torch, X, y, mu, ks, lik, noise, optimise_noise, th, stream)
         assert ginfo == winfo == 0, (call, ginfo, winfo)
-        assert abs(got - want) <= 1e-9 * abs(want), (call, got, want)
+        if n == 1 and lik == 1:
+            # one point: the profiled variance is 0 up to rounding, so ll is
+            # +inf or a large positive number in either implementation
+            assert got > 30 and want > 30
+        else:
+            assert abs(got - want) <= 1e-9 * abs(want) + 1e-12, (call, got, want)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(lib):
