@@ -260,14 +260,30 @@ def shape_problems(key):
     raise KeyError(key)
 
 
+def tune_shape(probs, mus, S):
+    """The autotuner's configuration for this batch (fgpu.autotune: each
+    candidate timed on a sample of the batch's largest problems)."""
+    from fgpu import autotune
+    wl = [autotune.Workload(q.X, q.y, mu, q.kspec, q.likelihood, q.noise, q.optimise_noise, S)
+          for q, mu in zip(probs, mus)]
+    dev, sms = autotune.device_identity()
+    cfg, ms, hit = autotune.tune(wl, device=dev, sms=sms)
+    return cfg, {"choice": cfg.name, "candidates_ms_per_sample_replay": ms, "from_cache": hit,
+                 "sample": "the batch's largest problems, 8 evaluations"}
+
+
 def measure_shape(key, torch, stream, steps, warmup, tpeak, cores, cpu_model, no_cpu):
     """Throughput, end-to-end rate, update roofline and a bounded CPU sample
-    of one benchmark shape: every particle of every problem in one batch plan."""
-    from fgpu import Engine, Plan
+    of one benchmark shape: every particle of every problem in one batch plan,
+    in the configuration the autotuner picks for the shape."""
+    from fgpu import Engine, Plan, autotune
     from fgpu.gpr import mean_vector
     probs, S, desc = shape_problems(key)
     mus = [mean_vector(q.mean, q.X, q.y) for q in probs]
-    engines = [Engine(q.X, q.y, mu, q.kspec, q.likelihood, q.noise, q.optimise_noise) for q, mu in zip(probs, mus)]
+    cfg, tuned = tune_shape(probs, mus, S)
+    with autotune.use(cfg):
+        engines = [Engine(q.X, q.y, mu, q.kspec, q.likelihood, q.noise, q.optimise_noise)
+                   for q, mu in zip(probs, mus)]
     flat = [e for e in engines for _ in range(S)]
     nth = max(e.ntheta for e in engines)
     plan = Plan(flat, ldtheta=nth)
@@ -304,12 +320,13 @@ def measure_shape(key, torch, stream, steps, warmup, tpeak, cores, cpu_model, no
         plan.run(th[warmup + k])
     e2e_s = (time.perf_counter() - t0) / steps
     tflops = sum(tensor_update_flops(q.N) * S for q in probs)
-    achieved = tflops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
+    achieved = tflops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 and cfg.trailing == "tcgen05" else None
     out = {"workload": desc, "problems_per_step": len(flat), "value": len(flat) / (ms * 1e-3), "unit": UNIT,
-           "ms_per_step": ms, "waves": nwaves, "workspace_arena_gb": arena / 1e9,
+           "ms_per_step": ms, "tuned": tuned, "waves": nwaves, "workspace_arena_gb": arena / 1e9,
            "e2e": {"value": len(flat) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": len(flat) * nth * 8,
                    "d2h_bytes_per_step": len(flat) * 12},
-           "roofline": {"bound": "tensor", "kernel": "k_ozaki_update", "achieved": achieved, "peak": tpeak,
+           "roofline": {"bound": "tensor", "kernel": "k_ozaki_update" if cfg.trailing == "tcgen05" else
+                        "k_update (FP64; no tensor-core roofline)", "achieved": achieved, "peak": tpeak,
                         "unit": "TFLOP/s", "frac": achieved / tpeak if achieved else None,
                         "update_ms_per_step": upd_ms, "update_launches": upd_n},
            "gpu_launches": launches * steps, "cholesky_failure_rate": fail}
@@ -324,27 +341,46 @@ def measure_shape(key, torch, stream, steps, warmup, tpeak, cores, cpu_model, no
     from oracle.build_ref import RefCPU
     order = sorted(range(len(probs)), key=lambda a: probs[a].N)
     pick = sorted({order[int(f * (len(order) - 1))] for f in (0.1, 0.5, 0.9)}) if len(probs) > 1 else [0]
-    avail = host_mem_available()
-    done, secs, names = 0, 0.0, []
+    done, secs, names, used = 0, 0.0, [], 0
     for a in pick:
         q = probs[a]
-        need = 2 * 8.0 * q.d * q.N * q.N
-        if avail and need > 0.4 * avail:
-            names.append(f"N={q.N} skipped ({need / 1e9:.0f} GB of tensors)")
+        threads, why = ref_cpu_threads(q, cores)
+        if threads < 1:
+            names.append(f"N={q.N} skipped ({why})")
             continue
         ref = RefCPU(q.X, q.y, mus[a], q.kspec, q.likelihood, q.noise, q.optimise_noise)
-        t = q.thetas(cores, seed=77)
+        t = q.thetas(threads, seed=77)
         t0 = time.perf_counter()
-        ref.loglik_batch(t, cores)
+        ref.loglik_batch(t, threads)
         secs += time.perf_counter() - t0
         ref.close()
-        done += cores
-        names.append(f"N={q.N}")
+        done += threads
+        used = max(used, threads)
+        names.append(f"N={q.N}: {threads} in parallel" + (f" ({why})" if why else ""))
     if done:
-        out["cpu_baseline"] = {"value": done / secs, "unit": UNIT, "cores": cores, "kind": "port",
-                               "sample": f"{done} particles ({', '.join(names)}), one per core, in {secs:.1f} s "
+        out["cpu_baseline"] = {"value": done / secs, "unit": UNIT, "cores": used, "kind": "port",
+                               "sample": f"{done} particles ({'; '.join(names)}), in {secs:.1f} s "
                                          f"({cpu_model}); C restatement of the reference's OpenMP CPU path"}
     return out
+
+
+def ref_cpu_threads(q, cores):
+    """Particles the C restatement can evaluate in parallel in host memory:
+    it holds two d x N x N tensors, and every particle thread its own copy of
+    a leaf's active-dimension slice (n x N x N, as the reference copies it)
+    and a few N x N matrices.  Returns (threads, reason when fewer than cores)."""
+    from fgpu.kernel_spec import parse_kspec
+    avail = host_mem_available() or 64e9
+    nn = 8.0 * q.N * q.N
+    tensors = 2 * q.d * nn
+    slices = [len(nd[2]) for nd in parse_kspec(q.kspec) if nd[0] == "leaf" and nd[1] in (1, 2)]
+    per_thread = (max(slices) if slices and max(slices) < q.d else 0) * nn + 5 * nn
+    room = 0.5 * avail - tensors
+    threads = int(min(cores, room // per_thread)) if room > 0 else 0
+    if threads >= cores:
+        return cores, ""
+    return threads, (f"{tensors / 1e9:.0f} GB of tensors + {per_thread / 1e9:.1f} GB per particle "
+                     f"against {avail / 1e9:.0f} GB of host memory")
 
 
 def main():
@@ -358,8 +394,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=0, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--trailing", default="tcgen05", choices=("tcgen05", "fp64"),
-                    help="trailing-update arithmetic of the Cholesky")
+    ap.add_argument("--trailing", default="auto", choices=("auto", "tcgen05", "fp64"),
+                    help="trailing-update arithmetic of the Cholesky (auto: the autotuner's choice)")
     ap.add_argument("--shapes", default="water_like_500,methanol_like_2000,atoms_33_ragged,large_n_10000",
                     help="other benchmark shapes measured after the headline ('none' to skip)")
     ap.add_argument("--shape-steps", type=int, default=3)
@@ -376,17 +412,21 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    from fgpu import Engine, Plan, synth
+    from fgpu import Engine, Plan, autotune, synth
     from fgpu.build import build_library
-    from fgpu.gpr import mean_vector, set_trailing_update
+    from fgpu.gpr import mean_vector
     build_library()
-    mode = args.trailing
-    set_trailing_update(mode)
-
     p = synth.config3()
     mu = mean_vector(p.mean, p.X, p.y)
-    eng = Engine(p.X, p.y, mu, p.kspec, p.likelihood, p.noise, p.optimise_noise)
     S = args.swarm
+    tuned = None
+    if args.trailing == "auto":
+        cfg, tuned = tune_shape([p], [mu], S)
+    else:
+        cfg = autotune.Config(args.trailing, "tc" if args.trailing == "tcgen05" else "fp64")
+    mode = cfg.trailing
+    with autotune.use(cfg):
+        eng = Engine(p.X, p.y, mu, p.kspec, p.likelihood, p.noise, p.optimise_noise)
     plan = Plan([eng] * S)
     nth = eng.ntheta
     total = args.warmup + args.steps
@@ -503,11 +543,11 @@ def main():
              "peak_gbs": hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks.get("hbm_gbs")
              else "fallback 6.8 TB/s (profiling recipe)"}
     build["hbm_frac"] = build["achieved_gbs"] / hbm if build["achieved_gbs"] else None
+    tpeak = peaks.get("bf16_tflops_sustained")
+    src = "MEASURED_PEAKS.json bf16_tflops_sustained (dense fp16/bf16 tensor, kernel timed inside a long step)"
+    if not tpeak:
+        tpeak, src = 1700.0, "fallback: 1.7 PFLOP/s sustained bf16 (profiling recipe)"
     if mode == "tcgen05":
-        tpeak = peaks.get("bf16_tflops_sustained")
-        src = "MEASURED_PEAKS.json bf16_tflops_sustained (dense fp16/bf16 tensor, kernel timed inside a long step)"
-        if not tpeak:
-            tpeak, src = 1700.0, "fallback: 1.7 PFLOP/s sustained bf16 (profiling recipe)"
         tflops = tensor_update_flops(p.N) * S
         achieved = tflops / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
         roof = {"bound": "tensor", "achieved": achieved, "peak": tpeak, "unit": "TFLOP/s",
@@ -540,7 +580,7 @@ def main():
             cpu = {"value": None, "unit": UNIT, "cores": cores, "kind": "port", "sample": f"failed: {exc}"}
     clocks = clk.summary()
     shapes = {}
-    if rank == 0 and mode == "tcgen05" and args.shapes != "none":
+    if rank == 0 and args.shapes != "none":
         cores, cpu_model = host_info()
         for key in args.shapes.split(","):
             try:
@@ -552,7 +592,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, shapes of the glycine-like config)",
             "config": workload_config(p, S, ws),
-            "trailing_update": mode,
+            "trailing_update": mode, "engine_config": cfg.name, "tuned": tuned,
             "roofline": roof, "build": build, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
             "plain": {"value": plain_v, "unit": UNIT, "particles": args.plain},

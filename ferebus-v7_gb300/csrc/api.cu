@@ -111,12 +111,21 @@ int compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>
 // Tensor-core build eligibility (tensor-core mode): every leaf rbf, periodic,
 // linear or constant; one or two rbf / periodic leaves whose feature columns,
 // each rounded up to 16, fit the 128 digit columns of the panel buffer.  The
-// environment variable FGPU_BUILD=fp64 keeps the FP64 dot-product build.
+// process-wide build mode (fgpu_set_build_mode; FGPU_BUILD=fp64 at load)
+// can keep the FP64 dot-product build instead.
+int g_build_mode = -1;  // 1: tensor-core build where eligible, 0: FP64 dot-product build
+int build_mode() {
+  if (g_build_mode < 0) {
+    const char* v = getenv("FGPU_BUILD");
+    g_build_mode = (v && (strcmp(v, "fp64") == 0 || strcmp(v, "0") == 0)) ? 0 : 1;
+  }
+  return g_build_mode;
+}
+
 void plan_tc_build(Spec& sp) {
   sp.tc_build = 0;
   sp.ndot = 0;
-  const char* v = getenv("FGPU_BUILD");
-  if (v && (strcmp(v, "fp64") == 0 || strcmp(v, "0") == 0)) return;
+  if (build_mode() == 0) return;
   int koff = 0;
   for (int l = 0; l < sp.nleaf; ++l) {
     const Leaf& L = sp.leaf[l];
@@ -882,6 +891,13 @@ int fgpu_create(fgpu_ctx** out, int N, int d, const double* X, const double* y, 
 }
 
 int fgpu_nparams(const fgpu_ctx* ctx) { return ctx ? ctx->ntheta : FGPU_EINVAL; }
+
+int fgpu_set_build_mode(int mode) {
+  const int prev = build_mode();
+  if (mode != 0 && mode != 1) return fail(FGPU_EINVAL, "build mode must be 0 (fp64) or 1 (tensor cores)");
+  g_build_mode = mode;
+  return prev;
+}
 
 int fgpu_set_trailing_update(int mode) {
   const int prev = default_mode();

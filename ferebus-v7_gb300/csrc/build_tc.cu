@@ -181,11 +181,14 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
   uint64_t* empty = full + NSTAGE;
   uint64_t* tfull = full + 2 * NSTAGE;
   uint64_t* tempty = tfull + 1;
-  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 2);
+  uint64_t* drain = tfull + 2;  // quiescing after a give-up
+  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 3);
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint32_t issued = 0;  // producer lane: k-chunks whose operand copies were issued
   if (tid == 0) {
     s_abort = 0;
+    mbar_init(drain, 1);
     for (int k = 0; k < NSTAGE; ++k) {
       mbar_init(&full[k], 1);
       mbar_init(&empty[k], 1);
@@ -227,6 +230,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
             mbar_expect_tx(&full[st], STAGE);
             tma_load_5d(As, P.tmap_a, 0, 0, 2 * (c0 + c), 0, ti, &full[st]);
             tma_load_5d(As + A_STAGE, P.tmap_b, 0, (tj & 1) * 2, 2 * (c0 + c), 0, tj >> 1, &full[st]);
+            issued = g + 1;
           }
           if (s_abort) break;
         }
@@ -358,8 +362,14 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
     }
   }
   __syncthreads();
-  if (s_abort && tid == 0) {
-    for (int q = 0; q < nprob; ++q) atomicExch(&probs[q].status[2], 1);
+  if (s_abort) {
+    // a bounded wait gave up: the copies and MMAs this CTA issued finish
+    // (bounded waits) before it frees its TMEM and exits
+    if (warp == BLD_EPI_WARPS && lane == 0) drain_ring(full, NSTAGE, issued);
+    if (warp == BLD_EPI_WARPS + 1 && lane == 0) drain_mmas(drain);
+    __syncthreads();
+    if (tid == 0)
+      for (int q = 0; q < nprob; ++q) atomicExch(&probs[q].status[2], 1);
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (warp == BLD_EPI_WARPS + 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));

@@ -175,7 +175,12 @@ __global__ void __launch_bounds__(256) k_build(const Prob* __restrict__ probs) {
   if (np > 0 && !mbar_wait(bar, 0)) s_fail = 1;
   __syncthreads();
   if (s_fail) {
-    if (tid == 0) atomicExch(&P.status[2], 1);  // copy engine did not answer: report, do not hang
+    // copy engine did not answer: report, do not hang; the copies land
+    // (bounded wait) before the block's shared memory is released
+    if (tid == 0) {
+      mbar_wait(bar, 0);
+      atomicExch(&P.status[2], 1);
+    }
     return;
   }
 
@@ -327,7 +332,10 @@ __global__ void __launch_bounds__(256) k_build_dot(const Prob* __restrict__ prob
   if (!mbar_wait(bar, 0)) s_fail = 1;
   __syncthreads();
   if (s_fail) {
-    if (tid == 0) atomicExch(&P.status[2], 1);
+    if (tid == 0) {
+      mbar_wait(bar, 0);  // the copies land (bounded) before the block's shared memory is released
+      atomicExch(&P.status[2], 1);
+    }
     return;
   }
   const double noise = P.optimise_noise ? P.theta[sp.nkparams] : P.noise;
@@ -760,5 +768,49 @@ extern "C" int fgpu_diag_exp(const double* x, double* y, int n) {
   }
   cudaFree(d);
   if (e != cudaSuccess) return internal_fail(FGPU_ECUDA, cudaGetErrorString(e));
+  return FGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// diagnostic: the kernels' bounded mbarrier wait giving up.  One warp waits
+// on a shared-memory mbarrier that nothing arrives on (arrive = 0) or that
+// its lane 0 has completed first (arrive = 1), with `polls` polls, through
+// the same helper the tensor-core kernels use, and records a give-up in
+// status[2] as they do.  Nothing asynchronous (copy, MMA) is issued, so
+// nothing is left in flight when the wait gives up.
+// ---------------------------------------------------------------------------
+namespace fgpu {
+__global__ void k_diag_wait(int* __restrict__ status, int polls, int arrive) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (threadIdx.x == 0 && arrive) mbar_arrive(&bar);
+  __syncwarp();
+  const bool ok = mbar_wait_n(&bar, 0, polls);
+  if (threadIdx.x == 0 && !ok) atomicExch(&status[2], 1);
+}
+}  // namespace fgpu
+
+extern "C" int fgpu_diag_wait(int polls, int arrive) {
+  using namespace fgpu;
+  internal_clear_error();
+  if (polls < 1 || polls > (1 << 22) || (arrive != 0 && arrive != 1))
+    return internal_fail(FGPU_EINVAL, "fgpu_diag_wait: polls must be in 1..2^22 and arrive 0 or 1");
+  int* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(int) * 4);
+  if (e != cudaSuccess) return internal_fail(FGPU_ENOMEM, cudaGetErrorString(e));
+  int h[4] = {0, 0, 0, 0};
+  if ((e = cudaMemset(d, 0, sizeof(int) * 4)) == cudaSuccess) {
+    k_diag_wait<<<1, 32>>>(d, polls, arrive);
+    internal_add_launches(1);
+    if ((e = cudaGetLastError()) == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  }
+  cudaFree(d);
+  if (e != cudaSuccess) return internal_fail(FGPU_ECUDA, cudaGetErrorString(e));
+  // the status word maps to the host error exactly as after an evaluation
+  if (h[2]) return internal_fail(FGPU_ETIMEOUT, "a bounded wait in a kernel gave up (copy or MMA)");
   return FGPU_OK;
 }

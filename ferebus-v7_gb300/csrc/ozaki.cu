@@ -137,9 +137,12 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
   uint64_t* tempty = tfull + 1;                     // [UPD_MMA_WARPS]: that warp's levels drained
   uint64_t* afull = tfull + 1 + UPD_MMA_WARPS;      // accumulator tile landed in shared memory
   uint64_t* aempty = afull + 1;                     // epilogue done with the accumulator tile
-  uint32_t* slot = reinterpret_cast<uint32_t*>(aempty + 1);
+  uint64_t* drain = aempty + 1;                     // quiescing after a give-up
+  uint32_t* slot = reinterpret_cast<uint32_t*>(drain + 1);
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint32_t issued = 0;  // producer lane: k-chunks whose operand copies were issued
+  int acc_it = -1;      // producer lane: tile whose accumulator copy was issued last
   if (tid == 0) {
     s_abort = 0;
     for (int k = 0; k < NSTAGE; ++k) {
@@ -150,6 +153,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
     for (int k = 0; k < UPD_MMA_WARPS; ++k) mbar_init(&tempty[k], 256);
     mbar_init(afull, 1);
     mbar_init(aempty, 256);
+    mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 9) {
@@ -186,6 +190,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
             bulk_g2s(hi_s, P.acc_hi + tile, ACC_HI_TILE, afull);
             bulk_g2s(lo_s, P.acc_lo + tile, ACC_LO_TILE, afull);
             acc_issued = true;
+            acc_it = (int)it;
           }
           const int st = g % NSTAGE;
           if (!mbar_wait(&empty[st], ((g / NSTAGE) & 1) ^ 1)) {
@@ -196,6 +201,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
           mbar_expect_tx(&full[st], STAGE);
           tma_load_5d(As, P.tmap_a, 0, 0, 2 * c, 0, ti, &full[st]);
           tma_load_5d(As + A_STAGE, P.tmap_bs, 0, (tj & 1) * 2, 0, 2 * c, tj >> 1, &full[st]);
+          issued = g + 1;
         }
         if (s_abort) break;
         if (!acc_issued) {
@@ -206,6 +212,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
           mbar_expect_tx(afull, ACC_HI_TILE + ACC_LO_TILE);
           bulk_g2s(hi_s, P.acc_hi + tile, ACC_HI_TILE, afull);
           bulk_g2s(lo_s, P.acc_lo + tile, ACC_LO_TILE, afull);
+          acc_it = (int)it;
         }
         ++it;
       }
@@ -340,9 +347,19 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
     }
   }
   __syncthreads();
-  if (s_abort && tid == 0) {
-    // a bounded wait gave up: flag every problem of this step
-    for (int q = 0; q < nprob; ++q) atomicExch(&probs[q].status[2], 1);
+  if (s_abort) {
+    // a bounded wait gave up: before the CTA frees its TMEM and exits, the
+    // operand and accumulator copies it issued land and its MMAs complete
+    // (each of these waits is bounded too), then every problem of this step
+    // is flagged
+    if (warp == 8 && lane == 0) {
+      drain_ring(full, NSTAGE, issued);
+      if (acc_it >= 0) mbar_wait(afull, (uint32_t)acc_it & 1);
+    }
+    if (warp == 9 && lane == 0) drain_mmas(drain);
+    __syncthreads();
+    if (tid == 0)
+      for (int q = 0; q < nprob; ++q) atomicExch(&probs[q].status[2], 1);
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (warp == 9) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
@@ -393,14 +410,17 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
   uint64_t* tempty = tfull + 2;             // [2]
   uint64_t* idf = tfull + 4;                // [4] tile id published
   uint64_t* ide = tfull + 8;                // [4] tile id read by the MMA lane and the 256 epilogue threads
-  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 12);
+  uint64_t* drain = tfull + 12;             // quiescing after a give-up
+  uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 13);
   __shared__ int s_abort;
   __shared__ int s_tile[4];
   __shared__ PotfShared<QW> s_potf;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nch = 2 * ns;
+  uint32_t issued = 0;  // producer lane: k-chunks whose operand copies were issued
   if (tid == 0) {
     s_abort = 0;
+    mbar_init(drain, 1);
     for (int k = 0; k < CPL_NSTAGE; ++k) {
       mbar_init(&full[k], 1);
       mbar_init(&empty[k], 1);
@@ -463,6 +483,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
           mbar_expect_tx(&full[st], CSTAGE);
           tma_load_5d(As, P.tmap_a, 0, 0, kg, 0, ti, &full[st]);
           tma_load_5d(As + A_STAGE, tb, 0, dq, 0, kg, s, &full[st]);  // rows c0+32dq .. +N-1
+          issued = g + 1;
         }
       }
     }
@@ -618,8 +639,14 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
     }
   }
   __syncthreads();
-  if (s_abort && tid == 0) {
-    for (int k = 0; k < nprob; ++k) atomicExch(&probs[k].status[2], 1);
+  if (s_abort) {
+    // a bounded wait gave up: the copies and MMAs this CTA issued finish
+    // (bounded waits) before it frees its TMEM and exits
+    if (warp == 8 && lane == 0) drain_ring(full, CPL_NSTAGE, issued);
+    if (warp == 9 && lane == 0) drain_mmas(drain);
+    __syncthreads();
+    if (tid == 0)
+      for (int k = 0; k < nprob; ++k) atomicExch(&probs[k].status[2], 1);
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (warp == 9) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
@@ -871,7 +898,11 @@ __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict_
   if (bad) atomicOr(&P.status[3], 1);
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (tid == 0 && s_fail) atomicExch(&P.status[2], 1);
+  if (tid == 0 && s_fail) {
+    mbar_wait(bar, 0);  // the coupling MMAs complete (bounded) before TMEM is freed
+    atomicExch(&P.status[2], 1);
+  }
+  __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
 }
 

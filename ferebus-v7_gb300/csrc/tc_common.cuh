@@ -25,8 +25,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int it = 0; it < (1 << 22); ++it) {
+// wait for the phase of `parity` to complete, giving up after `limit` polls
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, int limit) {
+  for (int it = 0; it < limit; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -36,6 +37,22 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     if (ok) return true;
   }
   return false;
+}
+// the kernels' bounded wait: 2^22 polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) { return mbar_wait_n(bar, parity, 1 << 22); }
+
+// After a bounded wait gave up: wait (bounded) until the copies issued into
+// a `nstage`-deep ring have landed, so that no copy writes this CTA's shared
+// memory after it exits.  `issued` counts the k-chunks whose copies were
+// issued; chunk c went to stage c % nstage and completes that stage's phase
+// c / nstage, and the last chunk of each stage is the only one that can
+// still be in flight (a stage is reissued only after its previous chunk was
+// consumed, i.e. had landed).
+__device__ __forceinline__ void drain_ring(uint64_t* full, int nstage, uint32_t issued) {
+  for (int st = 0; st < nstage && (uint32_t)st < issued; ++st) {
+    const uint32_t last = issued - 1 - ((issued - 1 - (uint32_t)st) % (uint32_t)nstage);
+    mbar_wait(&full[st], (last / nstage) & 1);
+  }
 }
 
 // one non-blocking probe of an mbarrier phase
@@ -75,6 +92,13 @@ __device__ __forceinline__ void mma_f16_desc(uint32_t d_tmem, uint64_t a, uint64
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
                : "memory");
+}
+// After a bounded wait gave up: one more commit tracks every MMA this thread
+// issued; waiting (bounded) on it means none still writes TMEM when the CTA
+// deallocates it.  `drain` is an mbarrier of count 1 used for nothing else.
+__device__ __forceinline__ void drain_mmas(uint64_t* drain) {
+  mma_commit(drain);
+  mbar_wait(drain, 0);
 }
 
 // round(x * 2^(55 - e)) for |x| <= 2^e, with integer operations only.

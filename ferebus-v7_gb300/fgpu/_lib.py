@@ -20,6 +20,7 @@ EXPORTS = (
     "fgpu_destroy", "fgpu_last_error", "fgpu_version", "fgpu_last_launch_count",
     "fgpu_plan_set_profiling", "fgpu_plan_stage_times", "fgpu_loglik_noalloc",
     "fgpu_set_trailing_update", "fgpu_diag_exp", "fgpu_plan_waves", "fgpu_plan_partition",
+    "fgpu_diag_wait", "fgpu_set_build_mode",
 )
 
 c_double_p = C.POINTER(C.c_double)
@@ -86,6 +87,10 @@ def load(path=None):
     lib.fgpu_plan_waves.restype = C.c_int
     lib.fgpu_plan_partition.argtypes = [C.POINTER(C.c_longlong), C.c_int, C.c_longlong, c_int_p, c_int_p]
     lib.fgpu_plan_partition.restype = C.c_int
+    lib.fgpu_diag_wait.argtypes = [C.c_int, C.c_int]
+    lib.fgpu_diag_wait.restype = C.c_int
+    lib.fgpu_set_build_mode.argtypes = [C.c_int]
+    lib.fgpu_set_build_mode.restype = C.c_int
     _lib = lib
     return lib
 

@@ -75,6 +75,11 @@ class Engine:
         _lib.check(self.lib.fgpu_grad(self.handle, _dp(th), th.size, C.byref(ll), _dp(g), C.byref(info)))
         return ll.value, g, info.value
 
+    def clone(self):
+        """A new context on the same training set, created under the current
+        process-wide trailing-update and build modes."""
+        return Engine(self._X, self._y, self._mu, self.kspec, self.likelihood, self.noise, self.optimise_noise)
+
     def close(self):
         if getattr(self, "handle", None):
             self.lib.fgpu_destroy(self.handle)
@@ -174,6 +179,15 @@ def plan_partition(nbytes, budget):
     nw = C.c_int()
     _lib.check(lib.fgpu_plan_partition(b, n, int(budget), w, C.byref(nw)))
     return list(w), nw.value
+
+
+def set_build_mode(mode):
+    """Kernel-matrix build for engines created afterwards: "tc" (default,
+    exact distances on the tensor cores where the kernel allows) or "fp64"
+    (the FP64 dot-product form).  Returns the previous mode name."""
+    lib = _lib.load()
+    prev = _lib.check(lib.fgpu_set_build_mode({"fp64": 0, "tc": 1}[mode]))
+    return {0: "fp64", 1: "tc"}[prev]
 
 
 def loglik_batch(engines, thetas):

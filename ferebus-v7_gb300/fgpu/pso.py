@@ -89,7 +89,7 @@ class LockstepPSO:
     engine is an ``fgpu.Engine`` (one training set).  Cost = -logL.
     """
 
-    def __init__(self, problems, config: SwarmConfig, seed=17, evaluate=None):
+    def __init__(self, problems, config: SwarmConfig, seed=17, evaluate=None, tune=False):
         self.cfg = config
         self.rng = np.random.default_rng(seed)
         self.engines = [p[0] for p in problems]
@@ -97,7 +97,18 @@ class LockstepPSO:
         self.ntheta = [len(b[0]) for b in self.boxes]
         S = config.swarm_size
         self.owner = np.repeat(np.arange(len(problems)), S)
+        self.tuned = None
         if evaluate is None:
+            if tune:
+                # the engine configuration fastest for this batch's shape
+                # (fgpu.autotune; timed once per shape, then cached on disk)
+                from . import autotune
+                wl = [autotune.Workload(e._X, e._y, e._mu, e.kspec, e.likelihood, e.noise, e.optimise_noise, S)
+                      for e in self.engines]
+                dev, sms = autotune.device_identity()
+                self.tuned, self.tune_ms, _ = autotune.tune(wl, device=dev, sms=sms)
+                with autotune.use(self.tuned):
+                    self.engines = [e.clone() for e in self.engines]
             plan = Plan([e for e in self.engines for _ in range(S)], ldtheta=max(self.ntheta))
             evaluate = plan.run
             self.plan = plan

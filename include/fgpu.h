@@ -83,6 +83,18 @@ int fgpu_nparams(const fgpu_ctx* ctx);
 #define FGPU_TRAILING_TCGEN05 1
 int fgpu_set_trailing_update(int mode);
 
+/* Kernel-matrix build for contexts created after the call (process-wide
+ * default; returns the previous setting): FGPU_BUILD_TC (default) forms the
+ * exact distances on the tensor cores where the kernel allows it (leaves
+ * rbf / periodic / linear / constant, at most two rbf-or-periodic leaves);
+ * FGPU_BUILD_FP64 keeps the FP64 dot-product build.  The environment
+ * variable FGPU_BUILD=fp64 selects FP64 at load.  Both give the likelihood
+ * to the parity tolerance; the autotuner picks between them per shape.  No
+ * counterpart in the reference. */
+#define FGPU_BUILD_FP64 0
+#define FGPU_BUILD_TC 1
+int fgpu_set_build_mode(int mode);
+
 /* Plain drop-in: one particle per call.  Replaces
  * GaussianProcessRegressor%log_likelihood (src/model/gpr/gpr.f90:291-307) ->
  * compute_R (gpr.f90:185-189) + Likelihood%ll (src/model/gpr/likelihood.f90:161-253).
@@ -188,6 +200,15 @@ int fgpu_plan_stage_times(fgpu_plan* plan, double* ms, int* count);
  * y[i] = exp(x[i]).  Diagnostic only, for checking it against the host libm;
  * synchronous.  The reference has no counterpart. */
 int fgpu_diag_exp(const double* x, double* y, int n);
+
+/* The kernels' bounded mbarrier wait, alone: one warp waits with `polls`
+ * polls (1 .. 2^22) on a barrier that nothing arrives on (arrive = 0), or
+ * that it completed itself first (arrive = 1).  Returns FGPU_ETIMEOUT when
+ * the wait gave up -- through the same status word and host mapping as an
+ * evaluation -- and FGPU_OK otherwise; nothing asynchronous is in flight,
+ * and the device stays usable.  Diagnostic only, synchronous; the reference
+ * has no counterpart. */
+int fgpu_diag_wait(int polls, int arrive);
 
 /* Thread-local message for the last failing call on this thread. */
 const char* fgpu_last_error(void);

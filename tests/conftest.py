@@ -35,10 +35,10 @@ def gpu_available():
 
 @pytest.fixture(scope="session")
 def lib():
-    """The built engine library (built here if it is missing)."""
+    """The built engine library (rebuilt here if a source is newer: the
+    build is incremental, so this is quick when it is up to date)."""
     from fgpu import build, _lib
-    if not os.path.exists(build.LIB_PATH):
-        build.build_library()
+    build.build_library()
     return _lib.load()
 
 
@@ -54,10 +54,15 @@ def parity_tol(ll_exact, ll_openblas, fp64_err):
     * The engine may be no further from the exact value than twice the worst
       of those FP64 evaluations (with a floor of 1e-11 |ll| for well
       conditioned K, where every FP64 evaluation is within a few ulp);
-    * wherever OpenBLAS itself is within 1e-9 |ll| of the exact value, the
-      engine must be too (the 1e-9 relative target).
+    * wherever the FP64 evaluations are all within 1e-9 |ll| of the exact
+      value -- K conditioned well enough that FP64 LAPACK meets the 1e-9
+      relative target -- the engine must meet it too.  The condition is
+      taken on all ten evaluations, not on OpenBLAS's value alone: one
+      evaluation can land close to the exact value by chance (the
+      methanol-like set at N=2000 has OpenBLAS 4e-11 from it where MKL and
+      the perturbed evaluations are 1.3e-8 away).
     """
     t = max(2.0 * fp64_err, 1e-11 * abs(ll_exact))
-    if abs(ll_openblas - ll_exact) <= 1e-9 * abs(ll_exact):
+    if fp64_err <= 1e-9 * abs(ll_exact):
         t = min(t, 1e-9 * abs(ll_exact))
     return t
