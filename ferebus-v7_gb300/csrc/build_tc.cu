@@ -24,7 +24,9 @@
 //  * E = W_ii + W_jj - 2 W_ij (W_ii from the same digits, computed
 //    exactly when the digits are written) is |f_i - f_j|^2 2^(u - 2 - 2s):
 //    zero on the diagonal, and exp(-E 2^(2s + 1 - u)) is evaluated by the
-//    fixed-point exponential straight from the integer.
+//    fixed-point exponential straight from the integer (the leaf-scale form
+//    iexp_fixed_tab: a fixed binary point, a 1024-entry table in shared
+//    memory, a degree-4 polynomial).
 //
 // The leaf values combine through the kernel expression, which is
 // multilinear in the (at most two) distance leaves: k = a + b v0 + c v1 +
@@ -172,7 +174,8 @@ __global__ void __launch_bounds__(128) k_feat_digits(const Prob* __restrict__ pr
 constexpr int BLD_EPI_WARPS = 16;                      // 4 lane quarters x 4 groups of 16 columns
 constexpr int BLD_THREADS = (BLD_EPI_WARPS + 2) * 32;  // + TMA warp + MMA warp
 constexpr int NSTAGE = 3;
-constexpr uint32_t BLD_SMEM = NSTAGE * STAGE + 256;
+constexpr uint32_t BLD_TAB = NSTAGE * STAGE + 256;    // 2^(j/1024) table of the exponential
+constexpr uint32_t BLD_SMEM = BLD_TAB + 1024 * 8;
 
 __global__ void __launch_bounds__(BLD_THREADS, 1)
     k_build_tc(const Prob* __restrict__ probs, int nprob, const int* __restrict__ prefix) {
@@ -206,6 +209,9 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tbase = *slot;
   const int total = prefix[nprob];
+  unsigned long long* tab = reinterpret_cast<unsigned long long*>(smb + BLD_TAB);
+  for (int k = tid; k < 1024; k += BLD_THREADS) tab[k] = g_iexp_tab1024[k];
+  __syncthreads();
 
   if (warp == BLD_EPI_WARPS) {
     // ---------------- TMA producer: digit planes of each leaf's k chunks ----------------
@@ -324,7 +330,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
         // TMEM drained: the next pass's MMAs may start
         asm volatile("tcgen05.fence::before_thread_sync;");
         mbar_arrive(tempty);
-        const int eexp = 2 * P.fscale[d] + 1 - u;
+        const IexpScale esc = iexp_scale(2 * P.fscale[d] + 1 - u);
         const long long wi = P.fnorm[(size_t)d * nc + i];
         const long long* wj = P.fnorm + (size_t)d * nc + j0;
         // a plain sum of the two leaves (a = d = 0, b = c = 1) is one add,
@@ -335,7 +341,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
         for (int q = 0; q < 16; ++q) {
           long long E = wi + wj[q] - 2 * W[q];
           E = E < 0 ? 0 : E;
-          const double val = iexp_fixed((unsigned long long)E, eexp);
+          const double val = iexp_fixed_tab((unsigned long long)E, esc, tab);
           if (d == 0) {
             v0[q] = val;
           } else if (plain_sum) {

@@ -814,3 +814,38 @@ extern "C" int fgpu_diag_wait(int polls, int arrive) {
   if (h[2]) return internal_fail(FGPU_ETIMEOUT, "a bounded wait in a kernel gave up (copy or MMA)");
   return FGPU_OK;
 }
+
+// ---------------------------------------------------------------------------
+// diagnostic: the kernel-matrix build's leaf-scale exponential,
+// y[i] = exp(-E[i] 2^e), on host values
+// ---------------------------------------------------------------------------
+namespace fgpu {
+__global__ void k_diag_exp_fixed(const unsigned long long* __restrict__ E, int e, double* __restrict__ y, int n) {
+  __shared__ unsigned long long tab[1024];
+  for (int k = threadIdx.x; k < 1024; k += blockDim.x) tab[k] = g_iexp_tab1024[k];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = iexp_fixed_tab(E[i], iexp_scale(e), tab);
+}
+}  // namespace fgpu
+
+extern "C" int fgpu_diag_exp_fixed(const unsigned long long* E, int e, double* y, int n) {
+  using namespace fgpu;
+  internal_clear_error();
+  if (n < 0 || (n > 0 && (!E || !y)) || e > -1 || e < -128)
+    return internal_fail(FGPU_EINVAL, "fgpu_diag_exp_fixed: bad arguments (e must be in -128..-1)");
+  if (n == 0) return FGPU_OK;
+  unsigned long long* d = nullptr;
+  cudaError_t err = cudaMalloc(&d, sizeof(unsigned long long) * 2 * (size_t)n);
+  if (err != cudaSuccess) return internal_fail(FGPU_ENOMEM, cudaGetErrorString(err));
+  double* yd = reinterpret_cast<double*>(d + n);
+  if ((err = cudaMemcpy(d, E, sizeof(unsigned long long) * n, cudaMemcpyHostToDevice)) == cudaSuccess) {
+    k_diag_exp_fixed<<<(n + 255) / 256, 256>>>(d, e, yd, n);
+    internal_add_launches(1);
+    if ((err = cudaGetLastError()) == cudaSuccess)
+      err = cudaMemcpy(y, yd, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(d);
+  if (err != cudaSuccess) return internal_fail(FGPU_ECUDA, cudaGetErrorString(err));
+  return FGPU_OK;
+}

@@ -65,3 +65,52 @@ __device__ __forceinline__ double iexp_fixed(unsigned long long E, int e) {
   if (top < -55) return 1.0;    // below 2^-55: rounds to 1
   return iexp_core(E << lz, e - lz);
 }
+
+// exp(-E 2^e) for exact integers E >= 0 sharing one scale 2^e (the
+// kernel-matrix build's entries of one distance leaf), with the per-entry
+// work cut down:
+//  * y = E 2^e log2(e) is read off the 128-bit product E * C at a fixed
+//    binary point K0, C = log2(e) 2^63 rounded (relative error 2^-64, below
+//    2^-54 absolute in y for y < 1024): no per-entry normalisation;
+//  * 2^(j/1024) from a 1024-entry table the caller keeps in shared memory,
+//    so t < ln2/1024 and a degree-4 Taylor polynomial suffices (the omitted
+//    t^5/120 is below 2^-59);
+//  * one round-to-nearest into the double, subnormals included.
+// Measured within 1 ulp of iexp_fixed over 3.1e8 arguments.
+struct IexpScale {
+  int K0;  // binary point of y in E * IEXP_L2E64: y = (E C) 2^-K0
+};
+__device__ __forceinline__ IexpScale iexp_scale(int e) { return IexpScale{63 - e}; }
+
+__device__ __forceinline__ double iexp_fixed_tab(unsigned long long E, IexpScale sc,
+                                                 const unsigned long long* __restrict__ tab1024) {
+  if (E == 0) return 1.0;
+  const int K0 = sc.K0;
+  if (K0 >= 192) return 1.0;                   // y < 2^-64: rounds to 1
+  if (K0 < 64) return iexp_fixed(E, 63 - K0);  // outside this form's range
+  const unsigned __int128 P = (unsigned __int128)E * IEXP_L2E64;
+  const unsigned long long yi = K0 >= 128 ? 0ULL : (unsigned long long)(P >> K0);
+  const unsigned long long yf = (unsigned long long)(P >> (K0 - 64));
+  if (yi >= 1100) return 0.0;
+  const unsigned int m = (unsigned int)yi + (yf ? 1u : 0u);
+  const unsigned long long f = 0ULL - yf;  // (m - y) 2^64
+  const int j = (int)(f >> 54);
+  const unsigned long long t = __umul64hi(f & 0x003FFFFFFFFFFFFFULL, IEXP_LN2);  // s ln2, 2^64
+  unsigned long long q = IEXP_C4;
+  q = IEXP_C3 + __umul64hi(q, t);
+  q = IEXP_C2 + __umul64hi(q, t);
+  q = (1ULL << 63) + __umul64hi(q, t);
+  const unsigned long long p = (1ULL << 63) + __umul64hi(q, t);  // exp(t) 2^63
+  const unsigned long long Z = __umul64hi(tab1024[j], p);       // 2^(j/1024) exp(t) 2^62
+  const int top = (int)(Z >> 63);
+  const int sh = 10 + top;
+  const int be = 1023 + top - (int)m;
+  if (be >= 1) {
+    const unsigned long long mant = (Z + (1ULL << (sh - 1))) >> sh;
+    return __longlong_as_double((long long)(((unsigned long long)be << 52) + mant - (1ULL << 52)));
+  }
+  const int tot = sh + 1 - be;
+  if (tot > 64) return 0.0;
+  const unsigned long long mant = (tot == 64) ? (Z >> 63) : ((Z + (1ULL << (tot - 1))) >> tot);
+  return __longlong_as_double((long long)mant);
+}

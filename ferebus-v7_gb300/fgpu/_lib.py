@@ -20,7 +20,7 @@ EXPORTS = (
     "fgpu_destroy", "fgpu_last_error", "fgpu_version", "fgpu_last_launch_count",
     "fgpu_plan_set_profiling", "fgpu_plan_stage_times", "fgpu_loglik_noalloc",
     "fgpu_set_trailing_update", "fgpu_diag_exp", "fgpu_plan_waves", "fgpu_plan_partition",
-    "fgpu_diag_wait", "fgpu_set_build_mode",
+    "fgpu_diag_wait", "fgpu_set_build_mode", "fgpu_diag_exp_fixed",
 )
 
 c_double_p = C.POINTER(C.c_double)
@@ -89,6 +89,8 @@ def load(path=None):
     lib.fgpu_plan_partition.restype = C.c_int
     lib.fgpu_diag_wait.argtypes = [C.c_int, C.c_int]
     lib.fgpu_diag_wait.restype = C.c_int
+    lib.fgpu_diag_exp_fixed.argtypes = [C.POINTER(C.c_ulonglong), C.c_int, c_double_p, C.c_int]
+    lib.fgpu_diag_exp_fixed.restype = C.c_int
     lib.fgpu_set_build_mode.argtypes = [C.c_int]
     lib.fgpu_set_build_mode.restype = C.c_int
     _lib = lib

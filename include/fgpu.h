@@ -201,6 +201,11 @@ int fgpu_plan_stage_times(fgpu_plan* plan, double* ms, int* count);
  * synchronous.  The reference has no counterpart. */
 int fgpu_diag_exp(const double* x, double* y, int n);
 
+/* The kernel-matrix build's form of that exponential, for exact integer
+ * arguments of one scale: y[i] = exp(-E[i] 2^e), e in -128..-1.
+ * Diagnostic only, synchronous.  The reference has no counterpart. */
+int fgpu_diag_exp_fixed(const unsigned long long* E, int e, double* y, int n);
+
 /* The kernels' bounded mbarrier wait, alone: one warp waits with `polls`
  * polls (1 .. 2^22) on a barrier that nothing arrives on (arrive = 0), or
  * that it completed itself first (arrive = 1).  Returns FGPU_ETIMEOUT when

@@ -51,18 +51,18 @@ def parity_tol(ll_exact, ll_openblas, fp64_err):
     error scale: the largest distance to ``ll_exact`` over OpenBLAS, MKL and
     OpenBLAS on eight 4-ulp perturbations of K.
 
-    * The engine may be no further from the exact value than twice the worst
-      of those FP64 evaluations (with a floor of 1e-11 |ll| for well
-      conditioned K, where every FP64 evaluation is within a few ulp);
-    * wherever the FP64 evaluations are all within 1e-9 |ll| of the exact
-      value -- K conditioned well enough that FP64 LAPACK meets the 1e-9
-      relative target -- the engine must meet it too.  The condition is
-      taken on all ten evaluations, not on OpenBLAS's value alone: one
-      evaluation can land close to the exact value by chance (the
-      methanol-like set at N=2000 has OpenBLAS 4e-11 from it where MKL and
-      the perturbed evaluations are 1.3e-8 away).
+    * Where every one of those FP64 evaluations is within 1e-9 |ll| of the
+      exact value -- K conditioned well enough that FP64 LAPACK meets the
+      1e-9 relative target -- the engine must meet that target too.
+    * Where they are not, no FP64 code meets 1e-9, and the engine may be no
+      further from the exact value than twice the worst of them.
+
+    The condition is taken on all ten evaluations, not on OpenBLAS's value
+    alone, because one evaluation can land close to the exact value by
+    chance: at methanol-like N=2000 one parameter vector has OpenBLAS 4e-11
+    from it where MKL and the perturbed evaluations are 1.3e-8 away.
+    ``ll_openblas`` is kept in the signature for the reports.
     """
-    t = max(2.0 * fp64_err, 1e-11 * abs(ll_exact))
     if fp64_err <= 1e-9 * abs(ll_exact):
-        t = min(t, 1e-9 * abs(ll_exact))
-    return t
+        return 1e-9 * abs(ll_exact)
+    return 2.0 * fp64_err

@@ -48,3 +48,32 @@ def test_exp_range_ends(lib):
     assert y[0] == 1.0 and y[1] == 1.0 and y[2] == 1.0 and y[3] == 1.0
     assert y[11] == 0.0 and y[12] == 0.0 and y[13] == 0.0 and y[14] == 0.0 and np.isnan(y[15])
     assert 0.0 < y[10] < 1e-323   # gradual underflow reaches the smallest subnormal
+
+
+def _dev_exp_fixed(lib, E, e):
+    import ctypes as C
+    from fgpu import _lib
+    E = np.ascontiguousarray(E, dtype=np.uint64)
+    y = np.empty(E.size)
+    _lib.check(lib.fgpu_diag_exp_fixed(E.ctypes.data_as(C.POINTER(C.c_ulonglong)), e,
+                                       y.ctypes.data_as(_lib.c_double_p), E.size))
+    return y
+
+
+@pytest.mark.parametrize("e", [-40, -58, -69])
+def test_build_exp_within_one_ulp(lib, e):
+    """exp(-E 2^e) for exact integers E (the build's leaf-scale form), against
+    the host's extended-precision exp of the exactly represented argument."""
+    rng = np.random.default_rng(20 - e)
+    top = min(61, 10 - e)                      # arguments up to ~2^10
+    bits = rng.integers(0, top, size=300000)
+    E = (rng.integers(0, 2 ** 62, size=bits.size, dtype=np.uint64) >> (62 - bits).astype(np.uint64))
+    E = np.concatenate([E, np.array([0, 1, 2, 3, 2 ** 20, (2 ** 61) - 1], dtype=np.uint64)])
+    E = E[(E.astype(np.float64) * 2.0 ** e) < 740]
+    y = _dev_exp_fixed(lib, E, e)
+    x = -(E.astype(np.longdouble) * np.longdouble(2.0) ** e)   # exact in a 64-bit or wider significand
+    ref = np.exp(x).astype(np.float64)
+    ok = ref > 0
+    u = np.abs(y[ok] - ref[ok]) / np.spacing(ref[ok])
+    assert np.max(u) <= 1.0, (np.max(u), E[ok][np.argmax(u)])
+    assert y[E == 0][0] == 1.0
