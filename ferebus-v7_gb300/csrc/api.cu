@@ -190,8 +190,7 @@ struct Workspace {
   // tensor-core mode
   int* escale = nullptr;
   double* pw2 = nullptr;
-  long long* acc_hi = nullptr;
-  int* acc_lo = nullptr;
+  long long* acc = nullptr;
   unsigned char* slices = nullptr;
   unsigned char* tmaps = nullptr;  // 4 x 128 B TMA tensor maps over slices (128-, 64-row boxes; 64, 32 rows, planes stacked)
   double* splanes = nullptr;       // theta-scaled planes (dot-product build)
@@ -340,8 +339,7 @@ void fill_prob(Prob& p, const fgpu_ctx* c, const double* theta_d, const Workspac
   p.nt128 = c->nt128;
   p.escale = ws.escale;
   p.pw2 = ws.pw2;
-  p.acc_hi = ws.acc_hi;
-  p.acc_lo = ws.acc_lo;
+  p.acc = ws.acc;
   p.slices = ws.slices;
   p.tmap_a = ws.tmaps;
   p.tmap_b = ws.tmaps ? ws.tmaps + 128 : nullptr;
@@ -629,8 +627,7 @@ size_t layout_workspace(const fgpu_ctx* c, unsigned char* base, Workspace& ws) {
   if (c->mode == 1) {
     take(ws.escale, sizeof(int) * nc);
     take(ws.pw2, sizeof(double) * nc);
-    take(ws.acc_hi, sizeof(long long) * acc_tiles(c->nt128) * ACC_TILE_ELEMS);
-    take(ws.acc_lo, sizeof(int) * acc_tiles(c->nt128) * ACC_TILE_ELEMS);
+    take(ws.acc, sizeof(long long) * acc_tiles(c->nt128) * ACC_TILE_ELEMS);
     take(ws.slices, (size_t)c->nt128 * NSLICE * SLICE_BYTES);
     take(ws.splanes, sizeof(double) * (size_t)std::max(c->spec.nplanes, 1) * nc);
     take(ws.norms, sizeof(double) * (size_t)MAX_LEAF * nc);

@@ -76,8 +76,8 @@ struct Prob {
   int nt128;                      // Nc / 128 (mode 1)
   int* escale;                    // Nc: per-row power-of-two scale e_i, |L_ik| <= 2^e_i
   double* pw2;                    // Nc: 2^(e_i - 31)
-  long long* acc_hi;              // Nc x Nc in 128 x 64 tiles: exact sums of products, high part
-  int* acc_lo;                    // low 24 bits (value = (hi * 2^24 + lo) * 2^(e_i + e_j - 62))
+  long long* acc;                 // lower-triangle 128 x 64 tiles: exact sums of products W, value
+                                  // W 2^(e_i + e_j - 62); |W| < 2^62 (Cauchy-Schwarz with the row scales)
   unsigned char* slices;          // nt128 x 7 x 32 KB: fp16 digit planes of the current panel
   const void* tmap_a;             // TMA tensor map over slices, box 8 x 128 rows x 2 kgroups x 7 planes
   const void* tmap_b;             // same, box of 64 rows
@@ -134,9 +134,10 @@ constexpr int NB = 128;
 constexpr int NSLICE = 7;                       // fp16 digit planes per FP64 value
 constexpr size_t SLICE_BYTES = 128 * 128 * 2;   // one digit plane of a 128-row x 128-k tile
 // The exact trailing sums are kept for lower-triangle tiles only (128 rows x
-// 64 columns, column-major inside): column tile tj holds row tiles
-// tj / 2 .. nt128 - 1, so a problem stores nt128 (nt128 + 1) tiles instead of
-// (2 nt128) nt128.  acc_tile is the tile's index in that packed order.
+// 64 columns, column-major inside), one int64 per element: column tile tj
+// holds row tiles tj / 2 .. nt128 - 1, so a problem stores nt128 (nt128 + 1)
+// tiles instead of (2 nt128) nt128.  acc_tile is the tile's index in that
+// packed order.
 __host__ __device__ inline size_t acc_tile(int ti, int tj, int nt128) {
   const long long q = tj >> 1, h = tj & 1;
   return (size_t)(2 * q * nt128 - q * (q - 1) + h * (nt128 - q) + (ti - q));

@@ -17,8 +17,10 @@
 //    L = p + q (at most 7 pairs x 128 terms x 129^2 < 2^24) is an exact
 //    integer in f32, so the 7 level accumulators in TMEM hold exact integers.
 //    Levels p + q > 6 (weights below 2^-62 of the row scales) are dropped.
-//  * The epilogue turns the 7 exact level sums into two int64 words and
-//    ADDS them to per-element integer accumulators in HBM: the trailing
+//  * The epilogue turns the 7 exact level sums into one int64 and ADDS it
+//    to a per-element integer accumulator in HBM (every partial sum of
+//    L_ik L_jk is below 2^(e_i + e_j) by Cauchy-Schwarz, i.e. below 2^62 in
+//    the accumulator's units, so 64 bits hold it exactly): the trailing
 //    matrix update is exact integer arithmetic, order independent, and uses
 //    no FP64 instruction.  When a block column becomes the next panel, one
 //    FP64 conversion per element subtracts the accumulated sum from K.
@@ -57,8 +59,9 @@ __global__ void k_scales(const Prob* __restrict__ probs) {
 }
 
 // ---------------------------------------------------------------------------
-// block column s: K_ij -= (hi 2^24 + lo) 2^(e_i + e_j - 62), rows [c0, Nc)
+// block column s: K_ij -= W_ij 2^(e_i + e_j - 62), rows [c0, Nc)
 // ---------------------------------------------------------------------------
+constexpr int PP_COLS = 4;  // columns per thread of the panel conversion (a 64-column tile holds 16 groups)
 __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ probs, int s) {
   const Prob& P = probs[blockIdx.z];
   if (P.mode != 1 || s >= P.nt128 || s == 0 || P.status[1]) return;
@@ -67,13 +70,23 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
   if (i >= P.Nc) return;
   const size_t ld = (size_t)P.ld;
   const int ei = P.escale[i] - 62;
-  for (int jj = 0; jj < 16; ++jj) {
-    const int j = c0 + blockIdx.y * 16 + jj;
-    const size_t a = (acc_tile(i >> 7, j >> 6, P.nt128) * 64 + (j & 63)) * 128 + (i & 127);
-    const double w = fixed_to_double(P.acc_hi[a], P.acc_lo[a], ei + P.escale[j]);
-    double* kp = P.K + (size_t)j * ld + i;
-    *kp = *kp - w;
+  // PP_COLS columns per thread, their loads issued together (the
+  // accumulators and K never overlap, which the compiler cannot know)
+  const int jb = c0 + blockIdx.y * PP_COLS;
+  const size_t a0 = (acc_tile(i >> 7, jb >> 6, P.nt128) * 64 + (jb & 63)) * 128 + (i & 127);
+  double* kp = P.K + (size_t)jb * ld + i;
+  long long w[PP_COLS];
+  int ej[PP_COLS];
+  double kv[PP_COLS];
+#pragma unroll
+  for (int jj = 0; jj < PP_COLS; ++jj) {
+    w[jj] = P.acc[a0 + (size_t)jj * 128];
+    kv[jj] = kp[(size_t)jj * ld];
+    ej[jj] = P.escale[jb + jj];
   }
+#pragma unroll
+  for (int jj = 0; jj < PP_COLS; ++jj)
+    kp[(size_t)jj * ld] = kv[jj] - fixed_to_double(w[jj] >> 24, (int)(w[jj] & 0xFFFFFF), ei + ej[jj]);
 }
 
 // ---------------------------------------------------------------------------
@@ -82,24 +95,23 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
 // Output tiles are 128 rows x 64 columns; a tile's 7 level sums occupy 448
 // TMEM columns.  Warp 8 (one lane) streams the digit planes of each k-chunk
 // of 16 by 5-D TMA into a 3-stage ring and bulk-copies the tile's
-// accumulators (96 KB) into shared memory as soon as the previous tile's
+// accumulators (64 KB) into shared memory as soon as the previous tile's
 // epilogue has released that buffer; warp 9 (one lane) issues the
 // chunk's 28 digit pairs as 10 tcgen05.mma with B's planes stacked along N
 // (upd_issue_chunk); warps 0-7 drain TMEM into registers, release it
 // (so the next tile's MMAs start), then add the tile to the accumulators
 // and write them back to HBM while the tensor cores work on the next tile.
 //
-// Accumulator per element: W = hi * 2^24 + lo, hi int64, lo in [0, 2^24),
-// value = W * 2^(e_i + e_j - 62); tile-major storage of the lower
+// Accumulator per element: W (int64), value W * 2^(e_i + e_j - 62);
+// |W| < 2^62 (see above); tile-major storage of the lower
 // triangle's 128 x 64 tiles (acc_tile), column-major inside.  Tiles of a
 // step are enumerated problem by problem (prefix table from the host),
 // column tile major, row tile minor.
 // ---------------------------------------------------------------------------
 constexpr int CH = 8;                                // k-chunks of 16 per 128-panel (one MMA each)
 constexpr int NSTAGE = 3;
-constexpr uint32_t ACC_HI_TILE = 128 * 64 * 8;       // accumulator tile, high words (64 KB)
-constexpr uint32_t ACC_LO_TILE = 128 * 64 * 4;       // low 24-bit words (32 KB)
-constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + ACC_HI_TILE + ACC_LO_TILE + 256;
+constexpr uint32_t ACC_TILE = 128 * 64 * 8;          // accumulator tile (64 KB)
+constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + ACC_TILE + 256;
 constexpr int UPD_MMA_WARPS = 1;
 constexpr int UPD_THREADS = 32 * (9 + UPD_MMA_WARPS);  // warps 0-7 epilogue, 8 TMA, 9 MMA issue
 
@@ -129,9 +141,8 @@ __device__ __forceinline__ void upd_issue_chunk(uint32_t tbase, uint64_t adesc, 
 __global__ void __launch_bounds__(UPD_THREADS, 1)
     k_ozaki_update(const Prob* __restrict__ probs, int nprob, int s, const int* __restrict__ prefix) {
   extern __shared__ __align__(1024) unsigned char smu[];
-  long long* hi_s = reinterpret_cast<long long*>(smu + NSTAGE * STAGE);
-  int* lo_s = reinterpret_cast<int*>(smu + NSTAGE * STAGE + ACC_HI_TILE);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smu + NSTAGE * STAGE + ACC_HI_TILE + ACC_LO_TILE);
+  long long* acc_s = reinterpret_cast<long long*>(smu + NSTAGE * STAGE);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smu + NSTAGE * STAGE + ACC_TILE);
   uint64_t* empty = full + NSTAGE;
   uint64_t* tfull = full + 2 * NSTAGE;
   uint64_t* tempty = tfull + 1;                     // [UPD_MMA_WARPS]: that warp's levels drained
@@ -186,9 +197,8 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
         const uint32_t apar = (it & 1) ^ 1;
         for (int c = 0; c < CH; ++c, ++g) {
           if (!acc_issued && mbar_test(aempty, apar)) {
-            mbar_expect_tx(afull, ACC_HI_TILE + ACC_LO_TILE);
-            bulk_g2s(hi_s, P.acc_hi + tile, ACC_HI_TILE, afull);
-            bulk_g2s(lo_s, P.acc_lo + tile, ACC_LO_TILE, afull);
+            mbar_expect_tx(afull, ACC_TILE);
+            bulk_g2s(acc_s, P.acc + tile, ACC_TILE, afull);
             acc_issued = true;
             acc_it = (int)it;
           }
@@ -209,9 +219,8 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
             s_abort = 1;
             break;
           }
-          mbar_expect_tx(afull, ACC_HI_TILE + ACC_LO_TILE);
-          bulk_g2s(hi_s, P.acc_hi + tile, ACC_HI_TILE, afull);
-          bulk_g2s(lo_s, P.acc_lo + tile, ACC_LO_TILE, afull);
+          mbar_expect_tx(afull, ACC_TILE);
+          bulk_g2s(acc_s, P.acc + tile, ACC_TILE, afull);
           acc_it = (int)it;
         }
         ++it;
@@ -271,15 +280,10 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
       asm volatile("tcgen05.fence::after_thread_sync;");
       // drain the level sums one MMA warp's levels at a time, releasing
       // them at once so that its MMAs for the next tile start while the
-      // other levels drain; W = sum_l S_l 2^(8 (6 - l)) is gathered as
-      // hi 2^24 + lo on the way (lo < 3 2^24 until normalised)
-      long long hv[32];
-      int lv[32];
+      // other levels drain; W = sum_l S_l 2^(48 - 8 l) is gathered on the way
+      long long wv[32];
 #pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        hv[q] = 0;
-        lv[q] = 0;
-      }
+      for (int q = 0; q < 32; ++q) wv[q] = 0;
 #pragma unroll
       for (int G = 0; G < UPD_MMA_WARPS; ++G) {
 #pragma unroll
@@ -301,28 +305,15 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
             for (int jj = 0; jj < 8; ++jj) {
               // levels 0 and 1 hold at most 2 x 128 x 128^2 = 2^22 in magnitude (|d| <= 128)
               const int S = l <= 1 ? small_f2i(__uint_as_float(v[l][jj])) : __float2int_rn(__uint_as_float(v[l][jj]));
-              long long& hq = hv[gq * 8 + jj];
-              int& lq = lv[gq * 8 + jj];
-              if (l <= 3) {
-                hq += (long long)S << (8 * (3 - l));
-              } else {  // split at 2^24: S 2^(8 (6 - l)) = (S >> 8 (l - 3)) 2^24 + (S mod 2^(8 (l - 3))) 2^(8 (6 - l))
-                hq += S >> (8 * (l - 3));
-                lq += (S & ((1 << (8 * (l - 3))) - 1)) << (8 * (6 - l));
-              }
+              wv[gq * 8 + jj] += (long long)S << (48 - 8 * l);
             }
           }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
         mbar_arrive(&tempty[G]);  // these TMEM columns are free for the next tile
       }
-#pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        hv[q] += lv[q] >> 24;
-        lv[q] &= 0xFFFFFF;
-      }
       const size_t tile = acc_tile(ti, tj, P.nt128) * ACC_TILE_ELEMS;
-      long long* gh = P.acc_hi + tile;
-      int* gl = P.acc_lo + tile;
+      long long* ga = P.acc + tile;
       const bool first = (s == 0);
       if (!first && !mbar_wait(afull, it & 1)) {
         s_abort = 1;
@@ -331,16 +322,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 #pragma unroll
       for (int q = 0; q < 32; ++q) {
         const int idx = (h * 32 + q) * 128 + r;
-        long long hi = hv[q];
-        long long lo = lv[q];
-        if (!first) {
-          hi += hi_s[idx];
-          lo += lo_s[idx];
-          hi += lo >> 24;
-          lo &= 0xFFFFFF;
-        }
-        gh[idx] = hi;
-        gl[idx] = (int)lo;
+        ga[idx] = first ? wv[q] : wv[q] + acc_s[idx];
       }
       if (!first) mbar_arrive(aempty);
       ++it;
@@ -978,7 +960,7 @@ cudaError_t launch_scales(const Prob* probs, int nprob, int max_nc, cudaStream_t
 cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s) {
   const int rows = max_nc - step * NB;
   if (step == 0 || rows <= 0) return cudaSuccess;
-  k_panel_prep<<<dim3((rows + 255) / 256, NB / 16, nprob), 256, 0, s>>>(probs, step);
+  k_panel_prep<<<dim3((rows + 255) / 256, NB / PP_COLS, nprob), 256, 0, s>>>(probs, step);
   return cudaGetLastError();
 }
 
