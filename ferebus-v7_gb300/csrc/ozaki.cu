@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
   }
 #pragma unroll
   for (int jj = 0; jj < PP_COLS; ++jj)
-    kp[(size_t)jj * ld] = kv[jj] - fixed_to_double(w[jj] >> 24, (int)(w[jj] & 0xFFFFFF), ei + ej[jj]);
+    kp[(size_t)jj * ld] = kv[jj] - w64_to_double(w[jj], ei + ej[jj]);
 }
 
 // ---------------------------------------------------------------------------
@@ -281,7 +281,9 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
       // drain the level sums one MMA warp's levels at a time, releasing
       // them at once so that its MMAs for the next tile start while the
       // other levels drain; W = sum_l S_l 2^(48 - 8 l) is gathered on the way
-      long long wv[32];
+      // unsigned: wrapping arithmetic (partial sums may pass 2^63, the total
+      // W stays below 2^62)
+      unsigned long long wv[32];
 #pragma unroll
       for (int q = 0; q < 32; ++q) wv[q] = 0;
 #pragma unroll
@@ -305,7 +307,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
             for (int jj = 0; jj < 8; ++jj) {
               // levels 0 and 1 hold at most 2 x 128 x 128^2 = 2^22 in magnitude (|d| <= 128)
               const int S = l <= 1 ? small_f2i(__uint_as_float(v[l][jj])) : __float2int_rn(__uint_as_float(v[l][jj]));
-              wv[gq * 8 + jj] += (long long)S << (48 - 8 * l);
+              wv[gq * 8 + jj] += (unsigned long long)(long long)S << (48 - 8 * l);
             }
           }
         }
@@ -322,7 +324,7 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 #pragma unroll
       for (int q = 0; q < 32; ++q) {
         const int idx = (h * 32 + q) * 128 + r;
-        ga[idx] = first ? wv[q] : wv[q] + acc_s[idx];
+        ga[idx] = (long long)(first ? wv[q] : wv[q] + (unsigned long long)acc_s[idx]);
       }
       if (!first) mbar_arrive(aempty);
       ++it;
@@ -594,14 +596,13 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) {
           const int ej = __shfl_sync(0xffffffffu, ecol, g * 8 + jj);
-          long long S[NSLICE];
+          int S[NSLICE];
 #pragma unroll
           for (int l = 0; l < NSLICE; ++l)  // level l sums (l + 1) x K products of |d| <= 128: <= 2^22 for (l + 1) K <= 256
             S[l] = (l + 1) * 32 * NQ <= 256 ? small_f2i(__uint_as_float(v[l][jj]))
-                                             : (long long)__float2int_rn(__uint_as_float(v[l][jj]));
-          const long long low = S[4] * 65536 + S[5] * 256 + S[6];
-          const long long hi = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
-          kv[jj] -= fixed_to_double(hi, (int)(low & 0xFFFFFF), ei + ej);
+                                             : __float2int_rn(__uint_as_float(v[l][jj]));
+          // |sum_k L_ik L_jk| <= sqrt(K_ii K_jj) < 2^(e_i + e_j): |W| < 2^62
+          kv[jj] -= w64_to_double(levels_to_w64(S), ei + ej);
         }
         if (live) {
 #pragma unroll
@@ -689,8 +690,9 @@ constexpr uint32_t TQ_SMEM = TQ_A_BYTES + TQ_B_BYTES + 64;
 // is d_p + 128, and G >> 48 is d_0 (|d_0| <= 128 when |x| <= 2^e).  A byte
 // u under the fp16 exponent bits 0x64 is the half 1024 + u, so one HSUB2 of
 // 1152 per pair of entries yields the digits exactly, with no conversion
-// instruction.  A top digit outside [-128, 128] breaks the row's scale
-// bound and sets *bad.
+// instruction; two byte permutes place a pair's bytes under the 0x64 bytes.
+// A top digit outside [-128, 128] breaks the row's scale bound and sets
+// *bad.
 __device__ __forceinline__ void digits8_packed(const double* x, int e, bool* bad, uint4 out[NSLICE]) {
   unsigned lo[8], hi[8];
 #pragma unroll
@@ -706,16 +708,17 @@ __device__ __forceinline__ void digits8_packed(const double* x, int e, bool* bad
     unsigned w[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
-      unsigned u0, u1;
-      if (p == 0) {
-        u0 = (unsigned)(((int)hi[2 * m] >> 16) + 128);
-        u1 = (unsigned)(((int)hi[2 * m + 1] >> 16) + 128);
+      unsigned bits;
+      if (p == 0) {  // d_0 + 128 may be 256: arithmetic, not a byte
+        const unsigned u0 = (unsigned)(((int)hi[2 * m] >> 16) + 128);
+        const unsigned u1 = (unsigned)(((int)hi[2 * m + 1] >> 16) + 128);
+        bits = (0x6400u + u0) | ((0x6400u + u1) << 16);
       } else {
-        const int q = 6 - p;  // byte of G
-        u0 = (q < 4 ? lo[2 * m] >> (8 * q) : hi[2 * m] >> (8 * (q - 4))) & 0xFFu;
-        u1 = (q < 4 ? lo[2 * m + 1] >> (8 * q) : hi[2 * m + 1] >> (8 * (q - 4))) & 0xFFu;
+        const int q = 6 - p;  // byte of G: byte q & 3 of the low or high word
+        const unsigned wa = q < 4 ? lo[2 * m] : hi[2 * m], wb = q < 4 ? lo[2 * m + 1] : hi[2 * m + 1];
+        const unsigned t = __byte_perm(wa, 0x64646464u, 0x4440u | (unsigned)(q & 3));  // [a_q, 64, 64, 64]
+        bits = __byte_perm(wb, t, 0x7054u | ((unsigned)(q & 3) << 8));                  // [a_q, 64, b_q, 64]
       }
-      const unsigned bits = (0x6400u + u0) | ((0x6400u + u1) << 16);
       const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&bits), off);
       w[m] = *reinterpret_cast<const unsigned*>(&h);
     }
@@ -835,13 +838,11 @@ __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict_
     if (fac) {
 #pragma unroll
       for (int jj = 0; jj < 8; ++jj) {
-        long long S[NSLICE];  // every level <= 7 x 16 x 128^2 < 2^22
+        int S[NSLICE];  // every level <= 7 x 16 x 128^2 < 2^22
 #pragma unroll
         for (int l = 0; l < NSLICE; ++l) S[l] = small_f2i(__uint_as_float(v[l][jj]));
-        const long long low = S[4] * 65536 + S[5] * 256 + S[6];
-        const long long hi = S[0] * 16777216 + S[1] * 65536 + S[2] * 256 + S[3] + (low >> 24);
         const int j = TQ_H + g * 8 + jj;
-        x[j] -= fixed_to_double(hi, (int)(low & 0xFFFFFF), er - 62 + P.escale[col0 + j]);
+        x[j] -= w64_to_double(levels_to_w64(S), er - 62 + P.escale[col0 + j]);
       }
     }
   }

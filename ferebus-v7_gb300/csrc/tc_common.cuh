@@ -146,33 +146,41 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
 }
 
-// (hi 2^24 + lo) 2^e rounded to the nearest double (ties to even) with
-// integer operations only: |hi| < 2^62, 0 <= lo < 2^24.  The same double as
-// fma((double)hi, 2^24, (double)lo) scaled by 2^e, without the FP64 pipe.
-// Results below 2^-1022 (never reached by the factor's scales) flush to 0.
-__device__ __forceinline__ double fixed_to_double(long long hi, int lo, int e) {
-  const __int128 v = (__int128)hi * 16777216 + lo;
-  if (v == 0) return 0.0;
-  const bool neg = v < 0;
-  unsigned __int128 a = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
-  const unsigned long long ah = (unsigned long long)(a >> 64), al = (unsigned long long)a;
-  const int lz = ah ? __clzll((long long)ah) : 64 + __clzll((long long)al);
-  a <<= lz;  // leading one at bit 127
-  const unsigned long long top = (unsigned long long)(a >> 64);
-  const bool sticky = (unsigned long long)a != 0;
-  unsigned long long mant = top >> 11;  // 53 bits
-  const unsigned long long rb = top & 0x7FF;
-  if (rb > 0x400 || (rb == 0x400 && (sticky || (mant & 1)))) ++mant;
-  int E = 127 - lz + e;  // value = 1.f 2^E
+// W 2^e rounded to the nearest double (ties to even) with integer
+// operations only, W a signed 64-bit integer: the same double as the exact
+// product correctly rounded, without the FP64 pipe.  Results below 2^-1022
+// (never reached by the factor's scales) flush to 0.
+__device__ __forceinline__ double w64_to_double(long long W, int e) {
+  if (W == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)W >> 63;
+  unsigned long long a = sgn ? 0ULL - (unsigned long long)W : (unsigned long long)W;
+  const int lz = __clzll((long long)a);
+  a <<= lz;  // leading one at bit 63
+  unsigned long long mant = a >> 11;  // 53 bits
+  const unsigned rb = (unsigned)a & 0x7FFu;
+  if (rb > 0x400u || (rb == 0x400u && (mant & 1))) ++mant;
+  int be = 63 - lz + e + 1023;  // biased exponent of 1.f
   if (mant >> 53) {
     mant >>= 1;
-    ++E;
+    ++be;
   }
-  const int be = E + 1023;
-  if (be <= 0) return neg ? -0.0 : 0.0;
-  if (be >= 2047) return __longlong_as_double(neg ? (long long)0xFFF0000000000000ULL : 0x7FF0000000000000LL);
-  return __longlong_as_double((long long)(((unsigned long long)neg << 63) | ((unsigned long long)be << 52) |
-                                          (mant & 0xFFFFFFFFFFFFFULL)));
+  if (be <= 0) return sgn ? -0.0 : 0.0;
+  if (be >= 2047) return __longlong_as_double((long long)((sgn << 63) | 0x7FF0000000000000ULL));
+  return __longlong_as_double((long long)((sgn << 63) | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFULL)));
+}
+
+// The exact integer W = sum_l S_l 256^(6 - l) of 7 level sums, in wrapping
+// 64-bit arithmetic: callers guarantee |W| < 2^63 (partial level sums may
+// exceed it; the wrapped total is still exact).
+__device__ __forceinline__ long long levels_to_w64(const int S[7]) {
+  unsigned long long w = (unsigned long long)(long long)S[6];
+  w += (unsigned long long)(long long)S[5] << 8;
+  w += (unsigned long long)(long long)S[4] << 16;
+  w += (unsigned long long)(long long)S[3] << 24;
+  w += (unsigned long long)(long long)S[2] << 32;
+  w += (unsigned long long)(long long)S[1] << 40;
+  w += (unsigned long long)(long long)S[0] << 48;
+  return (long long)w;
 }
 
 // an integer-valued float x with |x| <= 2^22 as an int, exactly, without a
