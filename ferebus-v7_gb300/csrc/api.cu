@@ -150,9 +150,11 @@ void plan_tc_build(Spec& sp) {
 // Per-step tile tables of the persistent tensor-core update: for step s,
 // prefix[s * (nprob + 1) + p] = tiles of problems < p.
 struct UpdSched {
-  int* prefix_dev = nullptr;
-  std::vector<int> totals;  // tiles per step
-  int stride = 0;           // nprob + 1
+  // trailing-update tiles of every step, packed (problem << 40 | row tile
+  // << 20 | column tile), problem by problem, column tile major
+  unsigned long long* tiles_dev = nullptr;
+  std::vector<size_t> tile_off;  // first tile of each step
+  std::vector<int> totals;       // tiles per step
   int num_sms = 0;
   int* build_prefix_dev = nullptr;  // nprob + 1: tiles of the tensor-core build
   int build_total = 0;
@@ -358,28 +360,33 @@ int build_sched(const std::vector<int>& nt128, const std::vector<int>& tc_build,
   const int nprob = (int)nt128.size();
   int ntmax = 0;
   for (int v : nt128) ntmax = std::max(ntmax, v);
-  u.stride = nprob + 1;
-  std::vector<int> h((size_t)std::max(ntmax, 1) * u.stride, 0);
+  // step st, problem p: m = nt128 - st - 1 trailing row tiles; column-tile
+  // pair q (tj = 2 (st + 1) + 2 q, + 1) holds row tiles st + 1 + q .. nt128 - 1
+  std::vector<unsigned long long> tl;
   u.totals.assign(std::max(ntmax, 1), 0);
+  u.tile_off.assign(std::max(ntmax, 1), 0);
   for (int st = 0; st < ntmax; ++st) {
-    int acc = 0;
+    u.tile_off[st] = tl.size();
     for (int p = 0; p < nprob; ++p) {
-      h[(size_t)st * u.stride + p] = acc;
       const int m = nt128[p] - st - 1;
-      if (m > 0) acc += m * (m + 1);
+      for (int q = 0; q < m; ++q)
+        for (int half = 0; half < 2; ++half)
+          for (int ti = st + 1 + q; ti < nt128[p]; ++ti)
+            tl.push_back(((unsigned long long)p << 40) | ((unsigned long long)ti << 20) |
+                         (unsigned long long)(2 * (st + 1) + 2 * q + half));
     }
-    h[(size_t)st * u.stride + nprob] = acc;
-    u.totals[st] = acc;
+    u.totals[st] = (int)(tl.size() - u.tile_off[st]);
   }
+  if (tl.empty()) tl.push_back(0);
   int dev = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&u.num_sms, cudaDevAttrMultiProcessorCount, dev));
   CK(cudaStreamCreateWithFlags(&u.side, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&u.fork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&u.join, cudaEventDisableTiming));
-  CK(cudaMalloc(&u.prefix_dev, sizeof(int) * h.size()));
-  if (track) track->push_back(u.prefix_dev);
-  CK(cudaMemcpy(u.prefix_dev, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&u.tiles_dev, sizeof(unsigned long long) * tl.size()));
+  if (track) track->push_back(u.tiles_dev);
+  CK(cudaMemcpy(u.tiles_dev, tl.data(), sizeof(unsigned long long) * tl.size(), cudaMemcpyHostToDevice));
   // couplings: the row tiles ti >= step of every problem, in the order the
   // CTAs take them: every problem's own row tile (which also carries the
   // next quarter's diagonal factor) first
@@ -475,7 +482,7 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
         STAGE(2, launch_trsm_quarter(probs_d, nprob, step, q, max_rows, s));  // also its digit planes
       }
       if (step + 1 < nt) {
-        STAGE(3, launch_ozaki_update(probs_d, nprob, step, nt, us->prefix_dev + (size_t)step * us->stride,
+        STAGE(3, launch_ozaki_update(probs_d, nprob, step, nt, us->tiles_dev + us->tile_off[step],
                                      us->totals[step], us->num_sms, s));
         // fork: the right-hand-side rows' FP64 update on the side branch,
         // beside the next step's panel conversion and quarter-0 factor
@@ -689,7 +696,7 @@ void free_worker(Worker* w) {
   cudaFree(w->ws.tmaps);
   cudaFree(w->theta_d);
   cudaFree(w->prob_d);
-  cudaFree(w->sched.prefix_dev);
+  cudaFree(w->sched.tiles_dev);
   cudaFree(w->sched.build_prefix_dev);
   cudaFree(w->sched.cpl_order_dev);
   cudaFree(w->sched.cpl_counter_dev);

@@ -134,23 +134,30 @@ constexpr int NB = 128;
 constexpr int NSLICE = 7;                       // fp16 digit planes per FP64 value
 constexpr size_t SLICE_BYTES = 128 * 128 * 2;   // one digit plane of a 128-row x 128-k tile
 // The exact trailing sums are kept for lower-triangle tiles only (128 rows x
-// 64 columns, column-major inside), one int64 per element: column tile tj
-// holds row tiles tj / 2 .. nt128 - 1, so a problem stores nt128 (nt128 + 1)
-// tiles instead of (2 nt128) nt128.  acc_tile is the tile's index in that
-// packed order.
+// 64 columns), one int64 per element: column tile tj holds row tiles tj / 2
+// .. nt128 - 1, so a problem stores nt128 (nt128 + 1) tiles instead of
+// (2 nt128) nt128.  acc_tile is the tile's index in that packed order.
+// Inside a tile the elements are grouped in 32 pieces of 2 KB, one per
+// (8-column group, 32-row quarter), each column-major (8 columns x 32 rows):
+// the piece one epilogue warp of the trailing update adds in a single bulk
+// reduction.  acc_elem is an element's index inside its tile.
 __host__ __device__ inline size_t acc_tile(int ti, int tj, int nt128) {
   const long long q = tj >> 1, h = tj & 1;
   return (size_t)(2 * q * nt128 - q * (q - 1) + h * (nt128 - q) + (ti - q));
 }
 inline size_t acc_tiles(int nt128) { return (size_t)nt128 * (nt128 + 1); }
+__host__ __device__ inline int acc_elem(int r, int c) {  // row r < 128, column c < 64 of the tile
+  return (((c >> 3) * 4 + (r >> 5)) << 8) + ((c & 7) << 5) + (r & 31);
+}
 constexpr size_t ACC_TILE_ELEMS = (size_t)NB * TB;
 
 cudaError_t launch_scales(const Prob* probs, int nprob, int max_nc, cudaStream_t s);
 cudaError_t launch_panel_prep(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
 // prefix: device table of nprob + 1 tile offsets for this step (tiles of
 // problem p at step s: m (m + 1), m = nt128_p - s - 1); total_tiles = prefix[nprob].
-cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, const int* prefix,
-                                int total_tiles, int num_sms, cudaStream_t s);
+// tiles: the step's trailing tiles, packed (problem << 40 | row tile << 20 | column tile)
+cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128,
+                                const unsigned long long* tiles, int total_tiles, int num_sms, cudaStream_t s);
 cudaError_t launch_border_update(const Prob* probs, int nprob, int step, int max_nc, cudaStream_t s);
 // four 32-column quarters per 128-panel (their digit planes are written by
 // the quarter panel solve): the tensor-core coupling of source quarters

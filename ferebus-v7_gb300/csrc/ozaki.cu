@@ -62,6 +62,7 @@ __global__ void k_scales(const Prob* __restrict__ probs) {
 // block column s: K_ij -= W_ij 2^(e_i + e_j - 62), rows [c0, Nc)
 // ---------------------------------------------------------------------------
 constexpr int PP_COLS = 4;  // columns per thread of the panel conversion (a 64-column tile holds 16 groups)
+static_assert(8 % PP_COLS == 0, "a thread's columns stay inside one 8-column group of an accumulator piece");
 __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ probs, int s) {
   const Prob& P = probs[blockIdx.z];
   if (P.mode != 1 || s >= P.nt128 || s == 0 || P.status[1]) return;
@@ -72,15 +73,15 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
   const int ei = P.escale[i] - 62;
   // PP_COLS columns per thread, their loads issued together (the
   // accumulators and K never overlap, which the compiler cannot know)
-  const int jb = c0 + blockIdx.y * PP_COLS;
-  const size_t a0 = (acc_tile(i >> 7, jb >> 6, P.nt128) * 64 + (jb & 63)) * 128 + (i & 127);
+  const int jb = c0 + blockIdx.y * PP_COLS;  // PP_COLS columns inside one 8-column group of a piece
+  const size_t a0 = acc_tile(i >> 7, jb >> 6, P.nt128) * ACC_TILE_ELEMS + acc_elem(i & 127, jb & 63);
   double* kp = P.K + (size_t)jb * ld + i;
   long long w[PP_COLS];
   int ej[PP_COLS];
   double kv[PP_COLS];
 #pragma unroll
   for (int jj = 0; jj < PP_COLS; ++jj) {
-    w[jj] = P.acc[a0 + (size_t)jj * 128];
+    w[jj] = P.acc[a0 + (size_t)jj * 32];
     kv[jj] = kp[(size_t)jj * ld];
     ej[jj] = P.escale[jb + jj];
   }
@@ -93,30 +94,45 @@ __global__ void __launch_bounds__(256) k_panel_prep(const Prob* __restrict__ pro
 // trailing update of the integer accumulators: persistent, warp-specialised
 //
 // Output tiles are 128 rows x 64 columns; a tile's 7 level sums occupy 448
-// TMEM columns.  Warp 8 (one lane) streams the digit planes of each k-chunk
-// of 16 by 5-D TMA into a 3-stage ring and bulk-copies the tile's
-// accumulators (64 KB) into shared memory as soon as the previous tile's
-// epilogue has released that buffer; warp 9 (one lane) issues the
-// chunk's 28 digit pairs as 10 tcgen05.mma with B's planes stacked along N
-// (upd_issue_chunk); warps 0-7 drain TMEM into registers, release it
-// (so the next tile's MMAs start), then add the tile to the accumulators
-// and write them back to HBM while the tensor cores work on the next tile.
+// TMEM columns.  Warp 16 (one lane) streams the digit planes of each
+// k-chunk of 16 by 5-D TMA into a 4-stage ring; warp 17 (one lane) issues
+// the chunk's 28 digit pairs as 10 tcgen05.mma with B's planes stacked
+// along N (upd_issue_chunk); warps 0-15 drain TMEM into registers (16
+// columns per thread, two rounds of TMEM loads), release it (so the next
+// tile's MMAs start), then stage each 8-column piece of the tile's exact
+// sums (2 KB, contiguous in the accumulator layout) in shared memory and
+// add it to the accumulators in HBM with one bulk reduction
+// (cp.reduce.async.bulk .add.u64: the L2 adds, exactly, modulo 2^64), while
+// the tensor cores work on the next tile.  The accumulators never pass
+// through the SM, which leaves the shared memory to a fourth operand stage.
+// (Per-element 64-bit reductions instead, with a fifth stage in the freed
+// staging memory, measured slower: the L2 takes them at about half the
+// bulk path's rate.)
 //
 // Accumulator per element: W (int64), value W * 2^(e_i + e_j - 62);
 // |W| < 2^62 (see above); tile-major storage of the lower
 // triangle's 128 x 64 tiles (acc_tile), column-major inside.  Tiles of a
-// step are enumerated problem by problem (prefix table from the host),
+// step are enumerated problem by problem (a packed list from the host),
 // column tile major, row tile minor.
 // ---------------------------------------------------------------------------
 constexpr int CH = 8;                                // k-chunks of 16 per 128-panel (one MMA each)
-constexpr int NSTAGE = 3;
-constexpr uint32_t ACC_TILE = 128 * 64 * 8;          // accumulator tile (64 KB)
-constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + ACC_TILE + 256;
-constexpr int UPD_MMA_WARPS = 1;
-constexpr int UPD_THREADS = 32 * (9 + UPD_MMA_WARPS);  // warps 0-7 epilogue, 8 TMA, 9 MMA issue
+constexpr int NSTAGE = 4;
+constexpr uint32_t UPD_PIECE = 8 * 32 * 8;  // one warp's staged accumulator piece: 8 columns x 32 rows (2 KB)
+constexpr int UPD_MMA_WARPS = 1;  // the epilogue's conversion below takes all 7 levels of a column group at once
+// epilogue warps: 4 TMEM lane quarters x UPD_EPI_WARPS / 4 column groups; the
+// tile's 7 levels drain in 64 / (UPD_EPI_WARPS / 4) / 8 rounds of 8 columns
+// per thread, and the next tile's MMAs wait for the last round
+constexpr int UPD_EPI_WARPS = 16;
+constexpr int UPD_COLS = 64 / (UPD_EPI_WARPS / 4);  // columns per epilogue thread
+constexpr int UPD_TMA_WARP = UPD_EPI_WARPS, UPD_MMA_WARP = UPD_EPI_WARPS + 1;
+constexpr int UPD_THREADS = 32 * (UPD_EPI_WARPS + 1 + UPD_MMA_WARPS);  // epilogue, TMA, MMA issue
+static_assert(UPD_COLS % 8 == 0 && UPD_EPI_WARPS % 4 == 0, "epilogue column groups of 8");
+constexpr uint32_t UPD_SMEM = NSTAGE * STAGE + UPD_EPI_WARPS * UPD_PIECE + 256;
+static_assert(UPD_SMEM <= 227 * 1024, "shared memory per CTA");
 
 // MMA-issuing warp of digit level l (one warp issues all levels)
 __host__ __device__ constexpr int upd_level_warp(int) { return 0; }
+static_assert(UPD_MMA_WARPS == 1, "the update epilogue converts all 7 levels of a column group in one pass");
 
 // one k-chunk of a tile with the B planes stacked along N: for A plane pp
 // the pairs (pp, q), q = 0 .. 6 - pp, accumulate into levels pp .. 6, whose
@@ -139,21 +155,19 @@ __device__ __forceinline__ void upd_issue_chunk(uint32_t tbase, uint64_t adesc, 
 }
 
 __global__ void __launch_bounds__(UPD_THREADS, 1)
-    k_ozaki_update(const Prob* __restrict__ probs, int nprob, int s, const int* __restrict__ prefix) {
+    k_ozaki_update(const Prob* __restrict__ probs, int nprob, int s, const unsigned long long* __restrict__ tiles,
+                   int total) {
   extern __shared__ __align__(1024) unsigned char smu[];
-  long long* acc_s = reinterpret_cast<long long*>(smu + NSTAGE * STAGE);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smu + NSTAGE * STAGE + ACC_TILE);
+  unsigned char* pieces = smu + NSTAGE * STAGE;  // [epilogue warp]: its staged accumulator piece
+  uint64_t* full = reinterpret_cast<uint64_t*>(smu + NSTAGE * STAGE + UPD_EPI_WARPS * UPD_PIECE);
   uint64_t* empty = full + NSTAGE;
   uint64_t* tfull = full + 2 * NSTAGE;
   uint64_t* tempty = tfull + 1;                     // [UPD_MMA_WARPS]: that warp's levels drained
-  uint64_t* afull = tfull + 1 + UPD_MMA_WARPS;      // accumulator tile landed in shared memory
-  uint64_t* aempty = afull + 1;                     // epilogue done with the accumulator tile
-  uint64_t* drain = aempty + 1;                     // quiescing after a give-up
+  uint64_t* drain = tempty + UPD_MMA_WARPS;         // quiescing after a give-up
   uint32_t* slot = reinterpret_cast<uint32_t*>(drain + 1);
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   uint32_t issued = 0;  // producer lane: k-chunks whose operand copies were issued
-  int acc_it = -1;      // producer lane: tile whose accumulator copy was issued last
   if (tid == 0) {
     s_abort = 0;
     for (int k = 0; k < NSTAGE; ++k) {
@@ -161,13 +175,11 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
       mbar_init(&empty[k], UPD_MMA_WARPS);  // a commit from each MMA warp
     }
     mbar_init(tfull, UPD_MMA_WARPS);
-    for (int k = 0; k < UPD_MMA_WARPS; ++k) mbar_init(&tempty[k], 256);
-    mbar_init(afull, 1);
-    mbar_init(aempty, 256);
+    for (int k = 0; k < UPD_MMA_WARPS; ++k) mbar_init(&tempty[k], UPD_EPI_WARPS * 32);
     mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 9) {
+  if (warp == UPD_MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -175,33 +187,26 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tbase = *slot;
-  const int total = prefix[nprob];
+  // tile t of the step: one load instead of a search over the problems
+  auto tile_of = [&](int t, int& p, int& ti, int& tj) {
+    const unsigned long long e = tiles[t];
+    p = (int)(e >> 40);
+    ti = (int)((e >> 20) & 0xFFFFF);
+    tj = (int)(e & 0xFFFFF);
+  };
 
-  if (warp == 8) {
+  if (warp == UPD_TMA_WARP) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
-      uint32_t g = 0, it = 0;
+      uint32_t g = 0;
       for (int t = blockIdx.x; t < total; t += gridDim.x) {
         int p, ti, tj;
-        decode_tile(probs, prefix, nprob, s, t, p, ti, tj);
+        tile_of(t, p, ti, tj);
         const Prob& P = probs[p];
         if (P.status[1]) continue;
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_bs) : "memory");
-        // The accumulator tile goes into its shared buffer as soon as the
-        // previous tile's epilogue has released it (polled between operand
-        // chunks, so the chunk loads never wait for the epilogue); step 0
-        // writes the accumulators without reading them.
-        bool acc_issued = (s == 0);
-        const size_t tile = acc_tile(ti, tj, P.nt128) * ACC_TILE_ELEMS;
-        const uint32_t apar = (it & 1) ^ 1;
         for (int c = 0; c < CH; ++c, ++g) {
-          if (!acc_issued && mbar_test(aempty, apar)) {
-            mbar_expect_tx(afull, ACC_TILE);
-            bulk_g2s(acc_s, P.acc + tile, ACC_TILE, afull);
-            acc_issued = true;
-            acc_it = (int)it;
-          }
           const int st = g % NSTAGE;
           if (!mbar_wait(&empty[st], ((g / NSTAGE) & 1) ^ 1)) {
             s_abort = 1;
@@ -214,28 +219,18 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
           issued = g + 1;
         }
         if (s_abort) break;
-        if (!acc_issued) {
-          if (!mbar_wait(aempty, apar)) {
-            s_abort = 1;
-            break;
-          }
-          mbar_expect_tx(afull, ACC_TILE);
-          bulk_g2s(acc_s, P.acc + tile, ACC_TILE, afull);
-          acc_it = (int)it;
-        }
-        ++it;
       }
     }
-  } else if (warp >= 9) {
+  } else if (warp >= UPD_MMA_WARP) {
     // ---------------- MMA issue ----------------
-    const int mw = warp - 9;
+    const int mw = warp - UPD_MMA_WARP;
     if (lane == 0) {
       uint32_t g = 0, it = 0;
       const uint64_t adesc0 = smem_desc(su32(smu), 2048, 128);
       const uint64_t bdesc0 = smem_desc(su32(smu) + A_STAGE, NSLICE * 1024, 128);  // [k-group][plane][row]
       for (int t = blockIdx.x; t < total; t += gridDim.x) {
         int p, ti, tj;
-        decode_tile(probs, prefix, nprob, s, t, p, ti, tj);
+        tile_of(t, p, ti, tj);
         if (probs[p].status[1]) continue;
         if (!mbar_wait(&tempty[mw], (it & 1) ^ 1)) {  // this warp's levels of the previous tile drained
           s_abort = 1;
@@ -263,14 +258,13 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
       }
     }
   } else {
-    // ---------------- epilogue (warps 0-7) ----------------
-    const int r = (warp & 3) * 32 + lane;  // TMEM lane = tile row
-    const int h = warp >> 2;               // column half
+    // ---------------- epilogue (warps 0 .. UPD_EPI_WARPS - 1) ----------------
+    const int h = warp >> 2;  // column group of UPD_COLS; TMEM lanes (tile rows) 32 (warp & 3) + lane
     const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
     uint32_t it = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
       int p, ti, tj;
-      decode_tile(probs, prefix, nprob, s, t, p, ti, tj);
+      tile_of(t, p, ti, tj);
       const Prob& P = probs[p];
       if (P.status[1]) continue;
       if (!mbar_wait(tfull, it & 1)) {
@@ -283,14 +277,12 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
       // other levels drain; W = sum_l S_l 2^(48 - 8 l) is gathered on the way
       // unsigned: wrapping arithmetic (partial sums may pass 2^63, the total
       // W stays below 2^62)
-      unsigned long long wv[32];
-#pragma unroll
-      for (int q = 0; q < 32; ++q) wv[q] = 0;
+      unsigned long long wv[UPD_COLS];
 #pragma unroll
       for (int G = 0; G < UPD_MMA_WARPS; ++G) {
 #pragma unroll
-        for (int gq = 0; gq < 4; ++gq) {
-          const int col0 = h * 32 + gq * 8;
+        for (int gq = 0; gq < UPD_COLS / 8; ++gq) {
+          const int col0 = h * UPD_COLS + gq * 8;
           uint32_t v[NSLICE][8];
 #pragma unroll
           for (int l = 0; l < NSLICE; ++l)
@@ -300,53 +292,88 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
                              "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
                            : "r"(tbase + lane_base + (uint32_t)(l * 64 + col0)));
           asm volatile("tcgen05.wait::ld.sync.aligned;");
+          // Exact integer level sums without the conversion unit (see
+          // level_bits): a sum outside [-2^22, 2^22) (up to 2^24 in
+          // principle, far rarer in practice) sends the warp through F2I for
+          // this group.
+          uint32_t band = 0xFFFFFFFFu, bor = 0u;
 #pragma unroll
-          for (int l = 0; l < NSLICE; ++l) {
-            if (upd_level_warp(l) != G) continue;
+          for (int l = 0; l < NSLICE; ++l)
 #pragma unroll
             for (int jj = 0; jj < 8; ++jj) {
-              // levels 0 and 1 hold at most 2 x 128 x 128^2 = 2^22 in magnitude (|d| <= 128)
-              const int S = l <= 1 ? small_f2i(__uint_as_float(v[l][jj])) : __float2int_rn(__uint_as_float(v[l][jj]));
-              wv[gq * 8 + jj] += (unsigned long long)(long long)S << (48 - 8 * l);
+              v[l][jj] = level_bits(v[l][jj]);
+              band &= v[l][jj];
+              bor |= v[l][jj];
             }
+          if (__any_sync(0xffffffffu, !level_bits_valid(band, bor))) {
+            // the level sums again from TMEM (not yet released), through F2I
+#pragma unroll
+            for (int l = 0; l < NSLICE; ++l)
+              asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                           : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
+                             "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
+                           : "r"(tbase + lane_base + (uint32_t)(l * 64 + col0)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+              int S[NSLICE];
+#pragma unroll
+              for (int l = 0; l < NSLICE; ++l) S[l] = __float2int_rn(__uint_as_float(v[l][jj]));
+              wv[gq * 8 + jj] = (unsigned long long)levels_to_w64(S);
+            }
+          } else {
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) wv[gq * 8 + jj] = (unsigned long long)level_bits_to_w64(v, jj);
           }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
         mbar_arrive(&tempty[G]);  // these TMEM columns are free for the next tile
       }
-      const size_t tile = acc_tile(ti, tj, P.nt128) * ACC_TILE_ELEMS;
-      long long* ga = P.acc + tile;
-      const bool first = (s == 0);
-      if (!first && !mbar_wait(afull, it & 1)) {
-        s_abort = 1;
-        break;
-      }
+      // each 8-column group of this warp's 32 rows is one contiguous 2 KB
+      // piece of the accumulator tile (acc_elem): staged in shared memory,
+      // then added to HBM by one bulk reduction from lane 0 (step 0 stores it)
+      long long* ga = P.acc + acc_tile(ti, tj, P.nt128) * ACC_TILE_ELEMS;
+      unsigned long long* stg = reinterpret_cast<unsigned long long*>(pieces + warp * UPD_PIECE);
 #pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        const int idx = (h * 32 + q) * 128 + r;
-        ga[idx] = (long long)(first ? wv[q] : wv[q] + (unsigned long long)acc_s[idx]);
+      for (int pc = 0; pc < UPD_COLS / 8; ++pc) {
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the last reduction has read the buffer
+        __syncwarp();
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) stg[jj * 32 + lane] = wv[pc * 8 + jj];
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // visible to the bulk copy
+        __syncwarp();
+        if (lane == 0) {
+          long long* dst = ga + acc_elem((warp & 3) * 32, h * UPD_COLS + pc * 8);
+          if (s == 0)
+            asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(su32(stg)),
+                         "r"(UPD_PIECE)
+                         : "memory");
+          else
+            asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.u64 [%0], [%1], %2;" ::"l"(dst),
+                         "r"(su32(stg)), "r"(UPD_PIECE)
+                         : "memory");
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        }
       }
-      if (!first) mbar_arrive(aempty);
       ++it;
     }
   }
+  // the accumulator reductions this warp issued complete before the CTA
+  // (and its staged pieces) goes away
+  if (warp < UPD_EPI_WARPS && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   __syncthreads();
   if (s_abort) {
     // a bounded wait gave up: before the CTA frees its TMEM and exits, the
-    // operand and accumulator copies it issued land and its MMAs complete
-    // (each of these waits is bounded too), then every problem of this step
-    // is flagged
-    if (warp == 8 && lane == 0) {
-      drain_ring(full, NSTAGE, issued);
-      if (acc_it >= 0) mbar_wait(afull, (uint32_t)acc_it & 1);
-    }
-    if (warp == 9 && lane == 0) drain_mmas(drain);
+    // operand copies it issued land and its MMAs complete (each of these
+    // waits is bounded too), then every problem of this step is flagged
+    if (warp == UPD_TMA_WARP && lane == 0) drain_ring(full, NSTAGE, issued);
+    if (warp == UPD_MMA_WARP && lane == 0) drain_mmas(drain);
     __syncthreads();
     if (tid == 0)
       for (int q = 0; q < nprob; ++q) atomicExch(&probs[q].status[2], 1);
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
-  if (warp == 9) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
+  if (warp == UPD_MMA_WARP) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
 }
 
 // ---------------------------------------------------------------------------
@@ -593,16 +620,44 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) kn[jj] = more ? kcol[(size_t)((g + 1) * 8 + jj) * ld] : 0.0;
         asm volatile("tcgen05.wait::ld.sync.aligned;");
+        // the exact level sums from their magic-added bits (see level_bits),
+        // in place: a sum outside [-2^22, 2^22) (possible only for N = 64,
+        // levels >= 3) sends the warp back to the level sums, still in TMEM,
+        // and F2I
+        uint32_t band = 0xFFFFFFFFu, bor = 0u;
+#pragma unroll
+        for (int l = 0; l < NSLICE; ++l)
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            v[l][jj] = level_bits(v[l][jj]);
+            band &= v[l][jj];
+            bor |= v[l][jj];
+          }
+        const bool slow = NQ > 1 && __any_sync(0xffffffffu, !level_bits_valid(band, bor));
+        if (slow) {
+#pragma unroll
+          for (int l = 0; l < NSLICE; ++l)
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
+                           "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
+                         : "r"(tbase + (uint32_t)buf * 256 + ((uint32_t)(lq * 32) << 16) +
+                               (uint32_t)(l * N + hf * NH + g * 8)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+        }
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) {
           const int ej = __shfl_sync(0xffffffffu, ecol, g * 8 + jj);
-          int S[NSLICE];
+          long long W;
+          if (slow) {
+            int S[NSLICE];
 #pragma unroll
-          for (int l = 0; l < NSLICE; ++l)  // level l sums (l + 1) x K products of |d| <= 128: <= 2^22 for (l + 1) K <= 256
-            S[l] = (l + 1) * 32 * NQ <= 256 ? small_f2i(__uint_as_float(v[l][jj]))
-                                             : __float2int_rn(__uint_as_float(v[l][jj]));
+            for (int l = 0; l < NSLICE; ++l) S[l] = __float2int_rn(__uint_as_float(v[l][jj]));
+            W = levels_to_w64(S);
+          } else {
+            W = level_bits_to_w64(v, jj);
+          }
           // |sum_k L_ik L_jk| <= sqrt(K_ii K_jj) < 2^(e_i + e_j): |W| < 2^62
-          kv[jj] -= w64_to_double(levels_to_w64(S), ei + ej);
+          kv[jj] -= w64_to_double(W, ei + ej);
         }
         if (live) {
 #pragma unroll
@@ -986,13 +1041,13 @@ cudaError_t launch_couple(const Prob* probs, int nprob, int step, int sq, int ns
   return cudaGetLastError();
 }
 
-cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128, const int* prefix,
-                                int total_tiles, int num_sms, cudaStream_t s) {
+cudaError_t launch_ozaki_update(const Prob* probs, int nprob, int step, int max_nt128,
+                                const unsigned long long* tiles, int total_tiles, int num_sms, cudaStream_t s) {
   cudaError_t e = set_attrs();
   if (e != cudaSuccess) return e;
   if (max_nt128 - step - 1 <= 0 || total_tiles <= 0) return cudaSuccess;
   const int grid = total_tiles < num_sms ? total_tiles : num_sms;
-  k_ozaki_update<<<grid, UPD_THREADS, UPD_SMEM, s>>>(probs, nprob, step, prefix);
+  k_ozaki_update<<<grid, UPD_THREADS, UPD_SMEM, s>>>(probs, nprob, step, tiles, total_tiles);
   return cudaGetLastError();
 }
 

@@ -183,6 +183,35 @@ __device__ __forceinline__ long long levels_to_w64(const int S[7]) {
   return (long long)w;
 }
 
+// Exact integer level sums without the conversion unit.  For an
+// integer-valued float x with -2^22 <= x < 2^22, x + 1.5 2^23 is exact and
+// its bits b = 0x4B000000 + (x + 2^22) agree with 0x4B000000 in bits 23..31;
+// any other x with |x| <= 2^24 changes those bits.  A group of such bits is
+// valid when the AND and the OR of the group both still agree there.
+__device__ __forceinline__ uint32_t level_bits(uint32_t v) {
+  return __float_as_uint(__uint_as_float(v) + 12582912.0f);
+}
+__device__ __forceinline__ bool level_bits_valid(uint32_t band, uint32_t bor) {
+  return (((band ^ 0x4B000000u) | (bor ^ 0x4B000000u)) >> 23) == 0u;
+}
+
+// W = sum_l x_l 256^(6 - l) from the valid bits b_l of column jj's 7 level
+// sums, in wrapping 64-bit arithmetic.  Adjacent levels pair up exactly in
+// 32 bits: b_l 256 + b_(l+1) = (x_l + 2^22) 256 + (x_(l+1) + 2^22) +
+// 0x4B000000 (the top byte of b_l leaves modulo 2^32, bit 23 is clear), below
+// 2^32; the offsets leave as one constant.
+constexpr unsigned long long LEVEL_BITS_BIAS =
+    (1ULL << 22) * 0x0001010101010101ULL + 0x4B000000ULL * ((1ULL << 40) + (1ULL << 24) + (1ULL << 8) + 1ULL);
+__device__ __forceinline__ long long level_bits_to_w64(const uint32_t (&b)[7][8], int jj) {
+  const uint32_t p01 = b[0][jj] * 256u + b[1][jj];
+  const uint32_t p23 = b[2][jj] * 256u + b[3][jj];
+  const uint32_t p45 = b[4][jj] * 256u + b[5][jj];
+  unsigned long long w = (unsigned long long)p45 * 256u + b[6][jj];
+  w += (unsigned long long)p23 << 24;
+  w += (unsigned long long)p01 << 40;
+  return (long long)(w - LEVEL_BITS_BIAS);
+}
+
 // an integer-valued float x with |x| <= 2^22 as an int, exactly, without a
 // conversion instruction: x + 1.5 * 2^23 lies in [2^23, 2^24], where the
 // float's low mantissa bits are x + 2^22 (one FADD and one IADD)
