@@ -156,7 +156,7 @@ struct UpdSched {
   std::vector<size_t> tile_off;  // first tile of each step
   std::vector<int> totals;       // tiles per step
   int num_sms = 0;
-  int* build_prefix_dev = nullptr;  // nprob + 1: tiles of the tensor-core build
+  unsigned long long* build_tiles_dev = nullptr;  // tiles of the tensor-core build, packed like `tiles_dev`
   int build_total = 0;
   std::vector<int> row_totals;      // per step: 128-row tiles ti >= step over all problems (couplings)
   int* cpl_order_dev = nullptr;     // per step: (problem << 16 | ti) of its row tiles, own row tile first
@@ -410,13 +410,22 @@ int build_sched(const std::vector<int>& nt128, const std::vector<int>& tc_build,
     CK(cudaMalloc(&u.cpl_counter_dev, sizeof(int) * u.ncounters));
     if (track) track->push_back(u.cpl_counter_dev);
   }
-  // tensor-core build: the whole lower triangle, nt128 (nt128 + 1) tiles of 128 x 64
-  std::vector<int> b(nprob + 1, 0);
-  for (int p = 0; p < nprob; ++p) b[p + 1] = b[p] + (tc_build[p] ? nt128[p] * (nt128[p] + 1) : 0);
-  u.build_total = b[nprob];
-  CK(cudaMalloc(&u.build_prefix_dev, sizeof(int) * b.size()));
-  if (track) track->push_back(u.build_prefix_dev);
-  CK(cudaMemcpy(u.build_prefix_dev, b.data(), sizeof(int) * b.size(), cudaMemcpyHostToDevice));
+  // tensor-core build: the whole lower triangle, nt128 (nt128 + 1) tiles of
+  // 128 x 64 per eligible problem, column-tile pair major, row tile minor
+  std::vector<unsigned long long> bl;
+  for (int p = 0; p < nprob; ++p) {
+    if (!tc_build[p]) continue;
+    for (int q = 0; q < nt128[p]; ++q)
+      for (int half = 0; half < 2; ++half)
+        for (int ti = q; ti < nt128[p]; ++ti)
+          bl.push_back(((unsigned long long)p << 40) | ((unsigned long long)ti << 20) |
+                       (unsigned long long)(2 * q + half));
+  }
+  u.build_total = (int)bl.size();
+  if (bl.empty()) bl.push_back(0);
+  CK(cudaMalloc(&u.build_tiles_dev, sizeof(unsigned long long) * bl.size()));
+  if (track) track->push_back(u.build_tiles_dev);
+  CK(cudaMemcpy(u.build_tiles_dev, bl.data(), sizeof(unsigned long long) * bl.size(), cudaMemcpyHostToDevice));
   return 0;
 }
 
@@ -457,7 +466,7 @@ int enqueue_eval(const Prob* probs_d, int nprob, int max_nsteps, int max_nplanes
     // right-hand-side rows of all
     STAGE(0, launch_build_dot(probs_d, nprob, max_nsteps, max_nplanes, s));
     if (us->build_total > 0)
-      STAGE(0, launch_build_tc(probs_d, nprob, us->build_prefix_dev, us->build_total, us->num_sms, s));
+      STAGE(0, launch_build_tc(probs_d, nprob, us->build_tiles_dev, us->build_total, us->num_sms, s));
     STAGE(0, launch_scales(probs_d, nprob, max_nc, s));
     const int max_rows = max_nc + TB;  // the tallest problem's ld: factor rows + right-hand sides
     bool joins = false;                // a side branch awaits its join
@@ -697,7 +706,7 @@ void free_worker(Worker* w) {
   cudaFree(w->theta_d);
   cudaFree(w->prob_d);
   cudaFree(w->sched.tiles_dev);
-  cudaFree(w->sched.build_prefix_dev);
+  cudaFree(w->sched.build_tiles_dev);
   cudaFree(w->sched.cpl_order_dev);
   cudaFree(w->sched.cpl_counter_dev);
   free_sched_sync(w->sched);

@@ -70,7 +70,24 @@ __device__ __forceinline__ long long assemble_w(const int S[NLEV], int u) {
   const long long H = (long long)S[0] * (1LL << 32) + (long long)S[1] * (1LL << 24) + (long long)S[2] * 65536 +
                       (long long)S[3] * 256 + S[4];
   const long long Lo = (long long)S[5] * 65536 + (long long)S[6] * 256 + S[7];
-  return H * (1LL << (u - 48)) + ((Lo + (1LL << (71 - u))) >> (72 - u));
+  return (long long)((unsigned long long)H << (u - 48)) + ((Lo + (1LL << (71 - u))) >> (72 - u));
+}
+
+// The same W from the magic-add bits b_L = 0x4B400000 + S_L of level sums
+// with |S_L| < 2^22 (level_bits): adjacent levels pair up in 32 bits
+// (b_L 256 + b_(L+1) = (S_L + 2^22) 256 + (S_(L+1) + 2^22) + 0x4B000000 <
+// 2^32, the top byte of b_L leaving modulo 2^32) and the offsets leave as two
+// constants, one for the top five levels and one for the last three.
+constexpr long long BUILD_BIAS_H = (1LL << 22) * 0x0101010101LL + 0x4B000000LL * ((1LL << 24) + (1LL << 8) + 1);
+constexpr long long BUILD_BIAS_LO = (1LL << 22) * 0x010101LL + 0x4B000000LL * ((1LL << 8) + 1);
+__device__ __forceinline__ long long assemble_w_bits(const uint32_t b[NLEV], int u) {
+  const uint32_t p01 = b[0] * 256u + b[1];
+  const uint32_t p23 = b[2] * 256u + b[3];
+  const uint32_t p56 = b[5] * 256u + b[6];
+  const long long H = (long long)(((unsigned long long)p01 << 24) + ((unsigned long long)p23 << 8) + b[4]) -
+                      BUILD_BIAS_H;  // sum_{L<=4} S_L 256^(4-L)
+  const long long Lo = (long long)(((unsigned long long)p56 << 8) + b[7]) - BUILD_BIAS_LO;
+  return (long long)((unsigned long long)H << (u - 48)) + ((Lo + (1LL << (71 - u))) >> (72 - u));
 }
 
 }  // namespace
@@ -174,11 +191,13 @@ __global__ void __launch_bounds__(128) k_feat_digits(const Prob* __restrict__ pr
 constexpr int BLD_EPI_WARPS = 16;                      // 4 lane quarters x 4 groups of 16 columns
 constexpr int BLD_THREADS = (BLD_EPI_WARPS + 2) * 32;  // + TMA warp + MMA warp
 constexpr int NSTAGE = 3;
-constexpr uint32_t BLD_TAB = NSTAGE * STAGE + 256;    // 2^(j/1024) table of the exponential
-constexpr uint32_t BLD_SMEM = BLD_TAB + 1024 * 8;
+constexpr uint32_t BLD_TAB = NSTAGE * STAGE + 256;    // the exponential's two tables (2 x 1024 x 8 B)
+constexpr uint32_t BLD_STASH = BLD_TAB + 2 * 1024 * 8;  // the first leaf's 16 values per epilogue thread
+constexpr uint32_t BLD_SMEM = BLD_STASH + BLD_EPI_WARPS * 32 * 16 * 8;
+static_assert(BLD_SMEM <= 227 * 1024, "shared memory per CTA");
 
 __global__ void __launch_bounds__(BLD_THREADS, 1)
-    k_build_tc(const Prob* __restrict__ probs, int nprob, const int* __restrict__ prefix) {
+    k_build_tc(const Prob* __restrict__ probs, int nprob, const unsigned long long* __restrict__ tiles, int total) {
   extern __shared__ __align__(1024) unsigned char smb[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smb + NSTAGE * STAGE);
   uint64_t* empty = full + NSTAGE;
@@ -208,10 +227,21 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tbase = *slot;
-  const int total = prefix[nprob];
   unsigned long long* tab = reinterpret_cast<unsigned long long*>(smb + BLD_TAB);
-  for (int k = tid; k < 1024; k += BLD_THREADS) tab[k] = g_iexp_tab1024[k];
+  unsigned long long* fine = tab + 1024;
+  double* stash = reinterpret_cast<double*>(smb + BLD_STASH);
+  for (int k = tid; k < 1024; k += BLD_THREADS) {
+    tab[k] = g_iexp_tab1024[k];
+    fine[k] = g_iexp_fine1024[k];
+  }
   __syncthreads();
+  // tile t: (problem << 40 | 128-row tile << 20 | 64-column tile), host-built
+  auto tile_of = [&](int t, int& p, int& ti, int& tj) {
+    const unsigned long long e = tiles[t];
+    p = (int)(e >> 40);
+    ti = (int)((e >> 20) & 0xFFFFF);
+    tj = (int)(e & 0xFFFFF);
+  };
 
   if (warp == BLD_EPI_WARPS) {
     // ---------------- TMA producer: digit planes of each leaf's k chunks ----------------
@@ -219,7 +249,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
       uint32_t g = 0;
       for (int t = blockIdx.x; t < total && !s_abort; t += gridDim.x) {
         int p, ti, tj;
-        decode_tile(probs, prefix, nprob, -1, t, p, ti, tj);
+        tile_of(t, p, ti, tj);
         const Prob& P = probs[p];
         const Spec& sp = *P.spec;
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(P.tmap_a) : "memory");
@@ -250,7 +280,7 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
       const uint64_t bdesc0 = smem_desc(su32(smb) + A_STAGE, 1024, 128);
       for (int t = blockIdx.x; t < total && !s_abort; t += gridDim.x) {
         int p, ti, tj;
-        decode_tile(probs, prefix, nprob, -1, t, p, ti, tj);
+        tile_of(t, p, ti, tj);
         const Spec& sp = *probs[p].spec;
         for (int d = 0; d < sp.ndot; ++d, ++it) {
           if (!mbar_wait(tempty, (it & 1) ^ 1)) {
@@ -291,13 +321,12 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
     uint32_t it = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
       int p, ti, tj;
-      decode_tile(probs, prefix, nprob, -1, t, p, ti, tj);
+      tile_of(t, p, ti, tj);
       const Prob& P = probs[p];
       const Spec& sp = *P.spec;
       const size_t nc = (size_t)P.Nc;
       const int i = ti * NB + r;
       const int j0 = tj * TB + h * 16;
-      double v0[16];
       bool stop = false;
       for (int d = 0; d < sp.ndot; ++d, ++it) {
         if (!mbar_wait(tfull, it & 1)) {
@@ -308,6 +337,11 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
         asm volatile("tcgen05.fence::after_thread_sync;");
         long long W[16];
         const int u = sp.dot_u[d];
+        // level sums of a leaf with at most 36 features stay below 2^22 (7
+        // digit pairs x 36 terms x 2^14): converted by the exact magic add
+        // (one FP32 add each, no conversion instruction), otherwise by F2I
+        const Leaf& LF = sp.leaf[sp.dot_leaf[d]];
+        const bool small = (LF.type == L_PERIODIC ? 2 * LF.n : LF.n) <= 36;
 #pragma unroll
         for (int gq = 0; gq < 2; ++gq) {
           uint32_t v[NLEV][8];
@@ -319,12 +353,22 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
                          : "r"(tbase + lane_base + (uint32_t)(l * 64 + h * 16 + gq * 8)));
           }
           asm volatile("tcgen05.wait::ld.sync.aligned;");
+          if (small) {
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            int S[NLEV];
+            for (int jj = 0; jj < 8; ++jj) {
+              uint32_t b[NLEV];
 #pragma unroll
-            for (int l = 0; l < NLEV; ++l) S[l] = __float2int_rn(__uint_as_float(v[l][jj]));
-            W[gq * 8 + jj] = assemble_w(S, u);
+              for (int l = 0; l < NLEV; ++l) b[l] = level_bits(v[l][jj]);
+              W[gq * 8 + jj] = assemble_w_bits(b, u);
+            }
+          } else {
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+              int S[NLEV];
+#pragma unroll
+              for (int l = 0; l < NLEV; ++l) S[l] = __float2int_rn(__uint_as_float(v[l][jj]));
+              W[gq * 8 + jj] = assemble_w(S, u);
+            }
           }
         }
         // TMEM drained: the next pass's MMAs may start
@@ -332,39 +376,58 @@ __global__ void __launch_bounds__(BLD_THREADS, 1)
         mbar_arrive(tempty);
         const IexpScale esc = iexp_scale(2 * P.fscale[d] + 1 - u);
         const long long wi = P.fnorm[(size_t)d * nc + i];
-        const long long* wj = P.fnorm + (size_t)d * nc + j0;
-        // a plain sum of the two leaves (a = d = 0, b = c = 1) is one add,
-        // the same double as the general form
-        const bool plain_sum = d > 0 && P.fcoef[0] == 0.0 && P.fcoef[1] == 1.0 && P.fcoef[2] == 1.0 &&
-                               P.fcoef[3] == 0.0;
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          long long E = wi + wj[q] - 2 * W[q];
+        // W_jj of this thread's 16 columns (the same for the whole warp), two at a time
+        const longlong2* wj2 = reinterpret_cast<const longlong2*>(P.fnorm + (size_t)d * nc + j0);
+        // The combination of the leaf values is chosen once per pass, outside
+        // the entry loop: a ternary inside it is compiled into both sides,
+        // and every FP64 operation costs this part's narrow FP64 pipe.  A
+        // plain sum of the two leaves (a = d = 0, b = c = 1) is one add, the
+        // same double as the general form.
+        const double ca = P.fcoef[0], cb = P.fcoef[1], cc = P.fcoef[2], cd = P.fcoef[3];
+        const int N = P.N;
+        double* K = P.K;
+        const size_t ld = (size_t)P.ld;
+        double kdiag = 0.0;  // this row's diagonal entry, when the tile holds it
+        // entry (i, j0 + q): lower triangle of the N x N block; identity padding
+        auto put = [&](int q, double kv) {
+          const int j = j0 + q;
+          if (j == i) kdiag = kv;
+          K[(size_t)j * ld + i] = (j > i || i >= N || j >= N) ? (i == j ? 1.0 : 0.0) : kv;
+        };
+        auto leaf = [&](int q) {
+          const longlong2 w2 = __ldg(wj2 + q / 2);
+          long long E = wi + ((q & 1) ? w2.y : w2.x) - 2 * W[q];
           E = E < 0 ? 0 : E;
-          const double val = iexp_fixed_tab((unsigned long long)E, esc, tab);
-          if (d == 0) {
-            v0[q] = val;
-          } else if (plain_sum) {
-            v0[q] = v0[q] + val;
-          } else {
+          return iexp_fixed_tab((unsigned long long)E, esc, tab, fine);
+        };
+        double* st = stash + tid;  // the first leaf's values, for the second pass
+        if (d < sp.ndot - 1) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) st[q * (BLD_EPI_WARPS * 32)] = leaf(q);
+        } else if (d == 0 && cb == 1.0 && ca == 0.0) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) put(q, leaf(q));
+        } else if (d == 0) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) put(q, fma(cb, leaf(q), ca));
+        } else if (ca == 0.0 && cb == 1.0 && cc == 1.0 && cd == 0.0) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) put(q, st[q * (BLD_EPI_WARPS * 32)] + leaf(q));
+        } else {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
             // second distance leaf: k = (d v0 + c) v1 + (b v0 + a)
-            v0[q] = fma(fma(P.fcoef[3], v0[q], P.fcoef[2]), val, fma(P.fcoef[1], v0[q], P.fcoef[0]));
+            const double v0 = st[q * (BLD_EPI_WARPS * 32)];
+            put(q, fma(fma(cd, v0, cc), leaf(q), fma(cb, v0, ca)));
           }
+        }
+        // the nugget on the diagonal (the loop stored the entry without it)
+        if (d == sp.ndot - 1 && i >= j0 && i < j0 + 16 && i < N) {
+          const double noise = P.optimise_noise ? P.theta[sp.nkparams] : P.noise;
+          K[(size_t)i * ld + i] = kdiag + noise * 1.0;
         }
       }
       if (stop) break;
-      const double noise = P.optimise_noise ? P.theta[sp.nkparams] : P.noise;
-      double* K = P.K;
-      const size_t ld = (size_t)P.ld;
-#pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        const int j = j0 + q;
-        double val = sp.ndot == 1 ? fma(P.fcoef[1], v0[q], P.fcoef[0]) : v0[q];
-        if (j > i) val = 0.0;
-        else if (i >= P.N || j >= P.N) val = (i == j) ? 1.0 : 0.0;
-        else if (i == j) val = val + noise * 1.0;
-        K[(size_t)j * ld + i] = val;
-      }
     }
   }
   __syncthreads();
@@ -389,13 +452,13 @@ cudaError_t launch_feat_digits(const Prob* probs, int nprob, int max_nt128, cuda
   return cudaGetLastError();
 }
 
-cudaError_t launch_build_tc(const Prob* probs, int nprob, const int* prefix, int total_tiles, int num_sms,
-                            cudaStream_t s) {
+cudaError_t launch_build_tc(const Prob* probs, int nprob, const unsigned long long* tiles, int total_tiles,
+                            int num_sms, cudaStream_t s) {
   cudaError_t e = ensure_smem_attr((const void*)k_build_tc, SMEM_BUILD_TC, BLD_SMEM);
   if (e != cudaSuccess) return e;
   if (total_tiles <= 0) return cudaSuccess;
   const int grid = total_tiles < num_sms ? total_tiles : num_sms;
-  k_build_tc<<<grid, BLD_THREADS, BLD_SMEM, s>>>(probs, nprob, prefix);
+  k_build_tc<<<grid, BLD_THREADS, BLD_SMEM, s>>>(probs, nprob, tiles, total_tiles);
   return cudaGetLastError();
 }
 

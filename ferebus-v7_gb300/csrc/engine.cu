@@ -821,11 +821,14 @@ extern "C" int fgpu_diag_wait(int polls, int arrive) {
 // ---------------------------------------------------------------------------
 namespace fgpu {
 __global__ void k_diag_exp_fixed(const unsigned long long* __restrict__ E, int e, double* __restrict__ y, int n) {
-  __shared__ unsigned long long tab[1024];
-  for (int k = threadIdx.x; k < 1024; k += blockDim.x) tab[k] = g_iexp_tab1024[k];
+  __shared__ unsigned long long tab[1024], fine[1024];
+  for (int k = threadIdx.x; k < 1024; k += blockDim.x) {
+    tab[k] = g_iexp_tab1024[k];
+    fine[k] = g_iexp_fine1024[k];
+  }
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = iexp_fixed_tab(E[i], iexp_scale(e), tab);
+  if (i < n) y[i] = iexp_fixed_tab(E[i], iexp_scale(e), tab, fine);
 }
 }  // namespace fgpu
 

@@ -171,10 +171,11 @@ cudaError_t launch_couple(const Prob* probs, int nprob, int step, int sq, int ns
 
 // Tensor-core kernel-matrix build (build_tc.cu): feature digit planes and
 // exact self products, then the persistent build of the lower triangle.
-// prefix: nprob + 1 tile offsets (nt128 (nt128 + 1) tiles per eligible problem).
+// tiles: the lower triangle's 128 x 64 tiles of every eligible problem,
+// packed (problem << 40 | row tile << 20 | column tile).
 cudaError_t launch_feat_digits(const Prob* probs, int nprob, int max_nt128, cudaStream_t s);
-cudaError_t launch_build_tc(const Prob* probs, int nprob, const int* prefix, int total_tiles, int num_sms,
-                            cudaStream_t s);
+cudaError_t launch_build_tc(const Prob* probs, int nprob, const unsigned long long* tiles, int total_tiles,
+                            int num_sms, cudaStream_t s);
 
 // Adjoint (grad.cu): identity rows below the right-hand-side tile turn into
 // L^-T during the sweep; K^-1 = L^-T (L^-T)^T; fused dK/dtheta pass.

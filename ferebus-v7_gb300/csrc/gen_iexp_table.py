@@ -11,7 +11,10 @@ Constants (computed here with mpmath at 80 digits, each rounded once):
   C2 .. C5        nearest integers to 2^63 / k!  (Taylor coefficients of exp)
   table[j]        nearest integer to 2^(j/256) 2^63, j = 0..255
   table1024[j]    nearest integer to 2^(j/1024) 2^63, j = 0..1023 (the
-                  kernel-matrix build's variant: degree-4 polynomial)
+                  kernel-matrix build's variant)
+  fine1024[k]     nearest integer to (2^(k/2^20) - 1) 2^64, k = 0..1023 (its
+                  second table: the rest below 2^-20 needs a degree-2
+                  polynomial only)
 
 Run: python gen_iexp_table.py > iexp_table.h
 """
@@ -23,6 +26,7 @@ LN2 = int(mp.nint(mp.log(2) * mp.mpf(2) ** 64))
 C = {k: int(mp.nint(mp.mpf(2) ** 63 / mp.factorial(k))) for k in range(2, 6)}
 tab = [int(mp.nint(mp.mpf(2) ** (mp.mpf(j) / 256 + 63))) for j in range(256)]
 tab1024 = [int(mp.nint(mp.mpf(2) ** (mp.mpf(j) / 1024 + 63))) for j in range(1024)]
+fine1024 = [int(mp.nint((mp.mpf(2) ** (mp.mpf(k) / 2 ** 20) - 1) * mp.mpf(2) ** 64)) for k in range(1024)]
 L2E64 = int(mp.nint(mp.mpf(2) ** 63 / mp.log(2)))
 print("// Generated by gen_iexp_table.py (constants of the fixed-point exponential).")
 print("#pragma once")
@@ -41,4 +45,9 @@ print("// 2^(j/1024) 2^63")
 print("static __device__ const unsigned long long g_iexp_tab1024[1024] = {")
 for j in range(0, 1024, 4):
     print("    " + ", ".join(f"0x{t:016x}ULL" for t in tab1024[j:j + 4]) + ",")
+print("};")
+print("// (2^(k/2^20) - 1) 2^64")
+print("static __device__ const unsigned long long g_iexp_fine1024[1024] = {")
+for k in range(0, 1024, 4):
+    print("    " + ", ".join(f"0x{t:016x}ULL" for t in fine1024[k:k + 4]) + ",")
 print("};")

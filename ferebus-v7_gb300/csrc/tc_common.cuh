@@ -1,7 +1,7 @@
 // Shared device helpers of the tcgen05 kernels: mbarriers with bounded waits,
 // shared-memory matrix descriptors, kind::f16 MMA issue and commit, TMA and
-// bulk copies, the FP64 -> 55-bit fixed-point conversion, and the tile
-// enumeration of a lower-triangular block range.
+// bulk copies, the FP64 -> 55-bit fixed-point conversion, and the exact
+// conversions of level sums.
 #pragma once
 #include "fgpu_internal.h"
 
@@ -216,31 +216,6 @@ __device__ __forceinline__ long long level_bits_to_w64(const uint32_t (&b)[7][8]
 // conversion instruction: x + 1.5 * 2^23 lies in [2^23, 2^24], where the
 // float's low mantissa bits are x + 2^22 (one FADD and one IADD)
 __device__ __forceinline__ int small_f2i(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
-
-// tile t of step s -> (problem, 128-row tile, 64-column tile); false if out of range
-__device__ __forceinline__ bool decode_tile(const Prob* __restrict__ probs, const int* __restrict__ prefix, int nprob,
-                                            int s, int t, int& p, int& ti, int& tj) {
-  if (t >= prefix[nprob]) return false;
-  int lo = 0, hi = nprob;  // largest p with prefix[p] <= t
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (prefix[mid] <= t) lo = mid; else hi = mid;
-  }
-  p = lo;
-  const int m = probs[p].nt128 - s - 1;
-  int r = t - prefix[p];
-  // column-tile pair q (tj = 2(s+1)+2q, +1) holds 2 (m - q) tiles
-  int q = 0;
-  while (r >= 2 * (m - q)) {
-    r -= 2 * (m - q);
-    ++q;
-  }
-  const int half = r >= (m - q) ? 1 : 0;
-  const int rr = r - half * (m - q);
-  tj = 2 * (s + 1) + 2 * q + half;
-  ti = s + 1 + q + rr;
-  return true;
-}
 
 }  // namespace
 }  // namespace fgpu
