@@ -706,14 +706,22 @@ __global__ void __launch_bounds__(256) k_border_update(const Prob* __restrict__ 
   __syncthreads();
   const int j = c0 + NB + blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= P.Nc) return;
-  double a0 = 0.0, a1 = 0.0;
-  for (int k = 0; k < NB; ++k) {
-    const double l = P.K[(size_t)(c0 + k) * ld + j];
-    a0 = fma(Z[0][k], l, a0);
-    a1 = fma(Z[1][k], l, a1);
+  // one or two right-hand sides, chosen outside the loop (FP64 operations
+  // for an absent second row would still cost the FP64 pipe)
+  if (P.nrhs > 1) {
+    double a0 = 0.0, a1 = 0.0;
+    for (int k = 0; k < NB; ++k) {
+      const double l = P.K[(size_t)(c0 + k) * ld + j];
+      a0 = fma(Z[0][k], l, a0);
+      a1 = fma(Z[1][k], l, a1);
+    }
+    P.K[(size_t)j * ld + P.Nc] -= a0;
+    P.K[(size_t)j * ld + P.Nc + 1] -= a1;
+  } else {
+    double a0 = 0.0;
+    for (int k = 0; k < NB; ++k) a0 = fma(Z[0][k], P.K[(size_t)(c0 + k) * ld + j], a0);
+    P.K[(size_t)j * ld + P.Nc] -= a0;
   }
-  P.K[(size_t)j * ld + P.Nc] -= a0;
-  if (P.nrhs > 1) P.K[(size_t)j * ld + P.Nc + 1] -= a1;
 }
 
 // ---------------------------------------------------------------------------
@@ -901,14 +909,18 @@ __global__ void __launch_bounds__(128, 4) k_trsm_quarter(const Prob* __restrict_
       }
     }
   }
-  if (live && !fac) {
-    // right-hand-side rows: the coupling in FP64
+  // right-hand-side rows: the coupling in FP64.  Only the warp holding a
+  // problem's right-hand-side rows enters (a warp-uniform branch), so the
+  // other warps do not issue these FP64 operations predicated off.
+  if (__any_sync(0xffffffffu, live && !fac)) {
+    if (live && !fac) {
 #pragma unroll
-    for (int j = TQ_H; j < QW; ++j) {
-      double a = x[j];
+      for (int j = TQ_H; j < QW; ++j) {
+        double a = x[j];
 #pragma unroll
-      for (int k = 0; k < TQ_H; ++k) a = fma(-x[k], L[j * QW + k], a);
-      x[j] = a;
+        for (int k = 0; k < TQ_H; ++k) a = fma(-x[k], L[j * QW + k], a);
+        x[j] = a;
+      }
     }
   }
   // second half
