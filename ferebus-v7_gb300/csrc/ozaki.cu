@@ -272,62 +272,56 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      // drain the level sums one MMA warp's levels at a time, releasing
-      // them at once so that its MMAs for the next tile start while the
-      // other levels drain; W = sum_l S_l 2^(48 - 8 l) is gathered on the way
-      // unsigned: wrapping arithmetic (partial sums may pass 2^63, the total
-      // W stays below 2^62)
+      // drain the 7 level sums of this thread's columns in groups of 8;
+      // W = sum_l S_l 2^(48 - 8 l) is gathered on the way in unsigned,
+      // wrapping arithmetic (partial sums may pass 2^63, the total W stays
+      // below 2^62)
       unsigned long long wv[UPD_COLS];
 #pragma unroll
-      for (int G = 0; G < UPD_MMA_WARPS; ++G) {
+      for (int gq = 0; gq < UPD_COLS / 8; ++gq) {
+        const int col0 = h * UPD_COLS + gq * 8;
+        uint32_t v[NSLICE][8];
 #pragma unroll
-        for (int gq = 0; gq < UPD_COLS / 8; ++gq) {
-          const int col0 = h * UPD_COLS + gq * 8;
-          uint32_t v[NSLICE][8];
+        for (int l = 0; l < NSLICE; ++l)
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                       : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
+                         "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
+                       : "r"(tbase + lane_base + (uint32_t)(l * 64 + col0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        // Exact integer level sums without the conversion unit (see
+        // level_bits) when every sum of the warp's group lies in (-2^22,
+        // 2^22) (up to 2^24 in principle, far rarer in practice); otherwise
+        // the warp converts this group with F2I.  The range is checked on the
+        // raw sums, so the conversion itself needs no second TMEM read and
+        // can follow the release below.
+        float mx = 0.0f;
+#pragma unroll
+        for (int l = 0; l < NSLICE; ++l)
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) mx = fmaxf(mx, fabsf(__uint_as_float(v[l][jj])));
+        const bool magic = __all_sync(0xffffffffu, mx < 4194304.0f);
+        if (gq == UPD_COLS / 8 - 1) {
+          // every level sum of the tile is in registers: the next tile's
+          // MMAs may overwrite these TMEM columns while the last group converts
+          asm volatile("tcgen05.fence::before_thread_sync;");
+          mbar_arrive(&tempty[0]);
+        }
+        if (magic) {
 #pragma unroll
           for (int l = 0; l < NSLICE; ++l)
-            if (upd_level_warp(l) == G)
-              asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                           : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
-                             "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
-                           : "r"(tbase + lane_base + (uint32_t)(l * 64 + col0)));
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
-          // Exact integer level sums without the conversion unit (see
-          // level_bits): a sum outside [-2^22, 2^22) (up to 2^24 in
-          // principle, far rarer in practice) sends the warp through F2I for
-          // this group.
-          uint32_t band = 0xFFFFFFFFu, bor = 0u;
 #pragma unroll
-          for (int l = 0; l < NSLICE; ++l)
+            for (int jj = 0; jj < 8; ++jj) v[l][jj] = level_bits(v[l][jj]);
 #pragma unroll
-            for (int jj = 0; jj < 8; ++jj) {
-              v[l][jj] = level_bits(v[l][jj]);
-              band &= v[l][jj];
-              bor |= v[l][jj];
-            }
-          if (__any_sync(0xffffffffu, !level_bits_valid(band, bor))) {
-            // the level sums again from TMEM (not yet released), through F2I
+          for (int jj = 0; jj < 8; ++jj) wv[gq * 8 + jj] = (unsigned long long)level_bits_to_w64(v, jj);
+        } else {
 #pragma unroll
-            for (int l = 0; l < NSLICE; ++l)
-              asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                           : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
-                             "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
-                           : "r"(tbase + lane_base + (uint32_t)(l * 64 + col0)));
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
+          for (int jj = 0; jj < 8; ++jj) {
+            int S[NSLICE];
 #pragma unroll
-            for (int jj = 0; jj < 8; ++jj) {
-              int S[NSLICE];
-#pragma unroll
-              for (int l = 0; l < NSLICE; ++l) S[l] = __float2int_rn(__uint_as_float(v[l][jj]));
-              wv[gq * 8 + jj] = (unsigned long long)levels_to_w64(S);
-            }
-          } else {
-#pragma unroll
-            for (int jj = 0; jj < 8; ++jj) wv[gq * 8 + jj] = (unsigned long long)level_bits_to_w64(v, jj);
+            for (int l = 0; l < NSLICE; ++l) S[l] = __float2int_rn(__uint_as_float(v[l][jj]));
+            wv[gq * 8 + jj] = (unsigned long long)levels_to_w64(S);
           }
         }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        mbar_arrive(&tempty[G]);  // these TMEM columns are free for the next tile
       }
       // each 8-column group of this warp's 32 rows is one contiguous 2 KB
       // piece of the accumulator tile (acc_elem): staged in shared memory,
