@@ -25,8 +25,8 @@
 //    exactly when the digits are written) is |f_i - f_j|^2 2^(u - 2 - 2s):
 //    zero on the diagonal, and exp(-E 2^(2s + 1 - u)) is evaluated by the
 //    fixed-point exponential straight from the integer (the leaf-scale form
-//    iexp_fixed_tab: a fixed binary point, a 1024-entry table in shared
-//    memory, a degree-4 polynomial).
+//    iexp_fixed_tab: a fixed binary point, two 1024-entry tables in shared
+//    memory, a degree-2 polynomial).
 //
 // The leaf values combine through the kernel expression, which is
 // multilinear in the (at most two) distance leaves: k = a + b v0 + c v1 +
@@ -34,7 +34,11 @@
 // problem, before the build).  The persistent kernel has the update's
 // structure: TMA producer warp, MMA warp, 16 epilogue warps (the epilogue's
 // integer work is what bounds the kernel, so it gets the warps); one pass per
-// distance leaf per 128 x 64 tile.
+// distance leaf per 128 x 64 tile, the first leaf's values kept in shared
+// memory for the second pass.  FP64 instructions run at 2 lanes per cycle
+// per SM on this part (FP32: 128), so the entry loop holds none but the one
+// add of a two-leaf sum: the combination is chosen once per pass, and the
+// nugget goes onto the one diagonal entry afterwards.
 #include "../../include/fgpu.h"
 #include "fgpu_internal.h"
 #include "iexp.cuh"
