@@ -76,11 +76,15 @@ def test_grad_edge_sizes(n, lib):
     assert close(g, rg)
 
 
-def test_grad_glycine_like_against_oracle_and_fd(lib):
+def test_grad_glycine_like_against_oracle_and_fd(lib, fp64_trailing):
     """The glycine-like configuration's kernel (rbf over 17 dims + periodic over
     7 dihedrals, concentrated likelihood, 24 parameters) at N=600 against the
     oracle, and the adjoint against central differences of the engine's own
-    log-likelihood (h = 1e-6 theta)."""
+    log-likelihood (h = 1e-6 theta, the benchmark configuration's step) on the
+    FP64 trailing update: the tensor-core path's rounding differs between
+    nearby theta by ~1e-13 |logL| (its smoothness is tested at full size
+    below with a step fitted to that), which a 2-point difference with this
+    step turns into ~1e-13 |logL| / h, the size of the allowance itself."""
     from fgpu import Engine, loglik_batch, synth
     p = synth.config3(600)
     mu = O.mean_vector("constant", p.X, p.y)
