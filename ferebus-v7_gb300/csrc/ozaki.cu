@@ -397,8 +397,10 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 // ---------------------------------------------------------------------------
 constexpr int CPL_NSTAGE = 3;
 constexpr uint32_t CPL_SMEM = CPL_NSTAGE * STAGE + 256;
-constexpr int CPL_THREADS = 352;  // warps 0-7 epilogue, 8 TMA, 9 MMA, 10 right-hand-side rows
-constexpr int CPL_EPI = 256;      // epilogue threads
+constexpr int CPL_EPI_WARPS = 16;                     // 4 TMEM lane quarters x 4 column groups
+constexpr int CPL_TMA_WARP = CPL_EPI_WARPS, CPL_MMA_WARP = CPL_EPI_WARPS + 1, CPL_RHS_WARP = CPL_EPI_WARPS + 2;
+constexpr int CPL_THREADS = 32 * (CPL_EPI_WARPS + 3);  // epilogue, TMA, MMA, right-hand-side rows
+constexpr int CPL_EPI = 32 * CPL_EPI_WARPS;            // epilogue threads
 
 template <int NQ>
 __global__ void __launch_bounds__(CPL_THREADS, 1)
@@ -414,7 +416,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
   uint64_t* tfull = full + 2 * CPL_NSTAGE;  // [2]
   uint64_t* tempty = tfull + 2;             // [2]
   uint64_t* idf = tfull + 4;                // [4] tile id published
-  uint64_t* ide = tfull + 8;                // [4] tile id read by the MMA lane and the 256 epilogue threads
+  uint64_t* ide = tfull + 8;                // [4] tile id read by the MMA lane and the epilogue threads
   uint64_t* drain = tfull + 12;             // quiescing after a give-up
   uint32_t* slot = reinterpret_cast<uint32_t*>(tfull + 13);
   __shared__ int s_abort;
@@ -440,7 +442,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 9) {
+  if (warp == CPL_MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
     return true;
   };
 
-  if (warp == 8) {
+  if (warp == CPL_TMA_WARP) {
     // ---------------- TMA producer (and tile fetcher) ----------------
     if (lane == 0) {
       uint32_t g = 0;
@@ -492,7 +494,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
         }
       }
     }
-  } else if (warp == 9) {
+  } else if (warp == CPL_MMA_WARP) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       uint32_t g = 0, it = 0;
@@ -540,7 +542,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
         mma_commit(&tfull[buf]);
       }
     }
-  } else if (warp == 10) {
+  } else if (warp == CPL_RHS_WARP) {
     // ---------------- right-hand-side rows (FP64), problems round-robin ----------------
     for (int p = blockIdx.x; p < nprob; p += gridDim.x) {
       const Prob& P = probs[p];
@@ -568,7 +570,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
     }
   } else {
     // ---------------- epilogue (warps 0-7): row = TMEM lane ----------------
-    constexpr int NH = N / 2;  // columns per warp
+    constexpr int NH = N / (CPL_EPI_WARPS / 4);  // columns per warp
     const int lq = warp & 3, hf = warp >> 2;
     uint32_t it = 0;
     for (uint32_t k = 0;; ++k, ++it) {
@@ -674,14 +676,14 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
   if (s_abort) {
     // a bounded wait gave up: the copies and MMAs this CTA issued finish
     // (bounded waits) before it frees its TMEM and exits
-    if (warp == 8 && lane == 0) drain_ring(full, CPL_NSTAGE, issued);
-    if (warp == 9 && lane == 0) drain_mmas(drain);
+    if (warp == CPL_TMA_WARP && lane == 0) drain_ring(full, CPL_NSTAGE, issued);
+    if (warp == CPL_MMA_WARP && lane == 0) drain_mmas(drain);
     __syncthreads();
     if (tid == 0)
       for (int k = 0; k < nprob; ++k) atomicExch(&probs[k].status[2], 1);
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
-  if (warp == 9) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
+  if (warp == CPL_MMA_WARP) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
 }
 
 // ---------------------------------------------------------------------------
