@@ -377,15 +377,15 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 // for rows i >= c0 + 32 dq, from the digit planes of the source quarters.
 // The panel uses three: quarter 0 -> 1, half 0 -> half 1, quarter 2 -> 3.
 // Persistent and warp-specialised like the trailing update: one lane of
-// warp 8 streams the k-chunks of each 128-row tile (A: 128 rows; B: the
-// destination's 32 NQ rows) through a 3-stage ring, one lane of warp 9
+// warp 16 streams the k-chunks of each 128-row tile (A: 128 rows; B: the
+// destination's 32 NQ rows) through a 3-stage ring, one lane of warp 17
 // issues the MMAs (N = 32 NQ) into TMEM (two buffers of 7 x 32 columns for
-// NQ = 1, one of 7 x 64 for NQ = 2), warps 0-7 drain the level sums (warps w
-// and w + 4 share TMEM lanes 32 (w % 4) and take half of the columns each,
-// in groups of 8 with the next group's K entries in flight; two warps per
-// SMSP hide the integer conversion's latency) and subtract the exactly
-// converted sums from K; warp 10 applies the same coupling to the
-// right-hand-side rows in FP64.  Once the epilogue warps have coupled a
+// NQ = 1, one of 7 x 64 for NQ = 2), warps 0-15 drain the level sums (warps
+// w, w + 4, w + 8, w + 12 share TMEM lanes 32 (w % 4) and take a quarter of
+// the columns each, in groups of 8 with the next group's K entries in
+// flight; four warps per SMSP hide the integer conversion's latency) and
+// subtract the exactly converted sums from K; warp 18 applies the same
+// coupling to the right-hand-side rows in FP64.  Once the epilogue warps have coupled a
 // problem's own 128-row tile (barrier 1), warps 0-3 factor quarter dq's
 // 32 x 32 diagonal block right there (barrier 2).
 // Tiles are handed out dynamically (an atomic counter over a host-built
@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
       }
     }
   } else {
-    // ---------------- epilogue (warps 0-7): row = TMEM lane ----------------
+    // ---------------- epilogue (warps 0-15): row = TMEM lane ----------------
     constexpr int NH = N / (CPL_EPI_WARPS / 4);  // columns per warp
     const int lq = warp & 3, hf = warp >> 2;
     uint32_t it = 0;
