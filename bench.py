@@ -595,7 +595,8 @@ def main():
             "trailing_update": mode, "engine_config": cfg.name, "tuned": tuned,
             "roofline": roof, "build": build, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
-            "plain": {"value": plain_v, "unit": UNIT, "particles": args.plain},
+            "plain": {"value": plain_v, "unit": UNIT, "particles": args.plain,
+                      "calls": "fgpu_loglik from one host thread, one call after the other"},
             "grad": {"ms": grad_s * 1e3, "fp64_flops": grad_flops,
                      "fp64_tflops": grad_flops / grad_s / 1e12, "fp64_peak_tflops": fp64_peak,
                      "frac": grad_flops / grad_s / 1e12 / fp64_peak,
