@@ -13,6 +13,14 @@ through the host.
   rank's {problem index: result}; every rank returns the merged dict.
 * ``global_best``: reduce per-rank (cost, position) of one shared swarm to
   the swarm's global best, ties broken by the lowest rank (particle order).
+* ``train_sharded``: the multi-atom training run over ranks: each rank
+  trains the atoms LPT gives it with a lockstep PSO (one batch plan for its
+  atoms' swarms per iteration), every swarm with its own random stream
+  seeded by the atom's index, and the per-atom results are all-gathered at
+  the end.  The result does not depend on the number of ranks.  This replaces
+  the reference's loop over atoms (app/main.f90:78-130) around the swarm
+  optimiser (src/optimiser/pso/pso.f90:382-472), which trains one atom
+  after the other on one node.
 """
 from __future__ import annotations
 
@@ -61,3 +69,30 @@ def global_best(cost, position, group=None):
     dist.all_gather_object(bucket, (float(cost), list(map(float, position))), group=group)
     best_rank = min(range(ws), key=lambda r: (bucket[r][0], r))
     return bucket[best_rank][0], bucket[best_rank][1], best_rank
+
+
+def train_sharded(problems, config, seed=17, evaluate_for=None, group=None, sizes=None):
+    """Train every problem (atom / property) on the ranks of ``group``.
+
+    problems: list of ``(engine, search_min, search_max)`` as for
+    ``fgpu.pso.LockstepPSO``; sizes: N per problem for the partition
+    (default: each engine's N); evaluate_for(indices) -> the batch evaluator
+    of the rank's problems (default: the engines' batch plan).  Returns on
+    every rank {problem index: {"theta", "cost", "evaluations", "failures",
+    "rank"}}.  Swarm a draws its random numbers from ``seed + a`` alone.
+    """
+    import torch.distributed as dist
+    from .pso import LockstepPSO
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    if sizes is None:
+        sizes = [p[0].N for p in problems]
+    mine = lpt_partition(sizes, world)[rank]
+    local = {}
+    if mine:
+        sub = [problems[i] for i in mine]
+        ev = evaluate_for(mine) if evaluate_for is not None else None
+        pso = LockstepPSO(sub, config, seeds=[seed + i for i in mine], evaluate=ev)
+        for i, (x, c), st in zip(mine, pso.run(), pso.states):
+            local[i] = {"theta": [float(v) for v in x], "cost": float(c), "evaluations": int(st.evaluations),
+                        "failures": int(st.failures), "rank": rank}
+    return allgather_results(local, group=group)

@@ -87,11 +87,21 @@ class LockstepPSO:
 
     ``problems`` is a list of ``(engine, search_min, search_max)``; each
     engine is an ``fgpu.Engine`` (one training set).  Cost = -logL.
+
+    Random numbers: one generator seeded by ``seed`` for all swarms, or, with
+    ``seeds`` (one per problem), a generator per swarm, so that a swarm's
+    trajectory does not depend on which other swarms share the batch (what
+    ``fgpu.partition.train_sharded`` relies on to give the same result on
+    any number of ranks).
     """
 
-    def __init__(self, problems, config: SwarmConfig, seed=17, evaluate=None, tune=False):
+    def __init__(self, problems, config: SwarmConfig, seed=17, evaluate=None, tune=False, seeds=None):
         self.cfg = config
         self.rng = np.random.default_rng(seed)
+        if seeds is not None and len(seeds) != len(problems):
+            raise ValueError("seeds: one per problem")
+        self.rngs = ([np.random.default_rng(x) for x in seeds] if seeds is not None
+                     else [self.rng] * len(problems))
         self.engines = [p[0] for p in problems]
         self.boxes = [(np.asarray(p[1], float), np.asarray(p[2], float)) for p in problems]
         self.ntheta = [len(b[0]) for b in self.boxes]
@@ -133,8 +143,8 @@ class LockstepPSO:
                 st = self.states[a]
                 i = k - a * S
                 delta = hi - lo
-                st.x[i] = self.rng.uniform(lo, hi)
-                st.v[i] = self.rng.uniform(-delta, delta)
+                st.x[i] = self.rngs[a].uniform(lo, hi)
+                st.v[i] = self.rngs[a].uniform(-delta, delta)
                 positions[k] = st.x[i]
                 st.failures += 1
             ll, info2 = self.evaluate_batch(positions)
@@ -155,10 +165,10 @@ class LockstepPSO:
         """init_pso: uniform positions in the box, velocities in +-(max - min)."""
         S = self.cfg.swarm_size
         self.states = []
-        for (lo, hi), n in zip(self.boxes, self.ntheta):
+        for a, ((lo, hi), n) in enumerate(zip(self.boxes, self.ntheta)):
             delta = hi - lo
-            x = self.rng.uniform(lo, hi, size=(S, n))
-            v = self.rng.uniform(-delta, delta, size=(S, n))
+            x = self.rngs[a].uniform(lo, hi, size=(S, n))
+            v = self.rngs[a].uniform(-delta, delta, size=(S, n))
             self.states.append(SwarmState(x=x, v=v, cost=np.full(S, np.inf), pbest_x=x.copy(),
                                           pbest_cost=np.full(S, np.inf), gbest_x=x[0].copy(),
                                           gbest_cost=np.inf, lo=lo, hi=hi))
@@ -177,10 +187,10 @@ class LockstepPSO:
     def step(self):
         """One global_swarm_update for every swarm, one batched evaluation."""
         cfg, S = self.cfg, self.cfg.swarm_size
-        for st in self.states:
+        for a, st in enumerate(self.states):
             n = st.x.shape[1]
-            r1 = self.rng.random((S, n))
-            r2 = self.rng.random((S, n))
+            r1 = self.rngs[a].random((S, n))
+            r2 = self.rngs[a].random((S, n))
             st.v = (cfg.inertia_weight * st.v + cfg.cognitive_learning_rate * r1 * (st.pbest_x - st.x)
                     + cfg.social_learning_rate * r2 * (st.gbest_x - st.x))
             st.x = st.x + st.v

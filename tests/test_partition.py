@@ -65,3 +65,75 @@ def test_gloo_two_ranks_gather_and_global_best():
     for rank, keys, cost, pos, who in out:
         assert keys == [0, 1, 2, 3, 4]
         assert cost == 9.0 and pos == [1.0, 2.0] and who == 1
+
+
+# -- the sharded multi-atom training driver ---------------------------------
+
+_SIZES = [600, 4000, 2500, 1200, 3300, 900]   # N per atom (partition weights)
+_NTH = [3, 4, 2, 5, 3, 4]                      # parameters per atom
+
+
+def _problems():
+    return [(None, np.full(n, 0.0), np.full(n, 1.0)) for n in _NTH]
+
+
+def _evaluate_for(indices):
+    """A deterministic stand-in for the engine: logL = -|theta - t_a|^2 with
+    a per-atom optimum, and a 'Cholesky failure' (info = 1) in a corner of
+    the box so that the retry rule runs."""
+    def evaluate(positions):
+        S = len(positions) // len(indices)
+        ll, info = [], []
+        for k, x in enumerate(positions):
+            a = indices[k // S]
+            t = 0.2 + 0.1 * a + 0.05 * np.arange(len(x))
+            ll.append(-float(np.sum((np.asarray(x) - t) ** 2)))
+            info.append(1 if x[0] > 0.97 else 0)
+        return np.array(ll), np.array(info, dtype=np.int32)
+    return evaluate
+
+
+def _sharded_worker(rank, world, port, q):
+    import torch.distributed as dist
+    from fgpu.partition import train_sharded
+    from fgpu.pso import SwarmConfig
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    cfg = SwarmConfig(swarm_size=6, iterations=12)
+    res = train_sharded(_problems(), cfg, seed=100, evaluate_for=_evaluate_for, sizes=_SIZES)
+    q.put((rank, res))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_sharded_training_matches_one_rank():
+    """train_sharded on 2 gloo ranks: every atom trained exactly once, on the
+    rank LPT gives it, and the results identical (bit for bit) to one
+    process training all atoms with the same per-atom random streams."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    from fgpu.pso import LockstepPSO, SwarmConfig
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_sharded_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = dict(q.get(timeout=120) for _ in range(2))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert out[0] == out[1]
+    res = out[0]
+    parts = lpt_partition(_SIZES, 2)
+    assert sorted(res) == list(range(len(_SIZES)))
+    for r, part in enumerate(parts):
+        assert all(res[i]["rank"] == r for i in part)
+    cfg = SwarmConfig(swarm_size=6, iterations=12)
+    allidx = list(range(len(_SIZES)))
+    one = LockstepPSO(_problems(), cfg, seeds=[100 + i for i in allidx], evaluate=_evaluate_for(allidx))
+    for i, ((x, c), st) in enumerate(zip(one.run(), one.states)):
+        assert res[i]["theta"] == [float(v) for v in x] and res[i]["cost"] == float(c)
+        assert res[i]["evaluations"] == st.evaluations and res[i]["failures"] == st.failures
+    assert sum(r["failures"] for r in res.values()) > 0   # the retry rule ran
