@@ -423,6 +423,9 @@ __global__ void __launch_bounds__(256) k_trsmw(const Prob* __restrict__ probs, i
   const int r0 = col0 + W + blockIdx.x * TB;
   if (col0 >= P.Nc || r0 >= row_end) return;
   if (*(volatile int*)&P.status[1]) return;
+  // the adjoint's identity rows: zero panel values before their own panel
+  // (see k_update), so their solve at earlier panels would leave zeros
+  if (r0 / TB > P.nsteps && r0 / TB - (P.nsteps + 1) > col0 / TB) return;
   constexpr int LDA = TB + 1;
   __shared__ double L[W * (W + 1)];
   __shared__ double B[W * LDA];
@@ -476,6 +479,11 @@ __global__ void __launch_bounds__(128) k_update(const Prob* __restrict__ probs, 
   const int ti = step + 1 + blockIdx.x, tj = step + 1 + blockIdx.y;
   const int last = P.nrt ? P.nrt - 1 : P.nsteps;
   if (step >= P.nsteps || tj >= P.nsteps || ti > last || ti < tj) return;
+  // The adjoint's identity rows (row tiles after the right-hand-side tile):
+  // tile nsteps + 1 + q starts as the unit rows of tile q, whose panel values
+  // stay exactly zero before panel q (L^-1 is lower triangular), so there
+  // is nothing to subtract at earlier steps.
+  if (ti > P.nsteps && ti - (P.nsteps + 1) > step) return;
   if (*(volatile int*)&P.status[1]) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* As = reinterpret_cast<double*>(smem_raw);  // [k][m]
