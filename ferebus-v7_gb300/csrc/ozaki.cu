@@ -137,19 +137,25 @@ static_assert(UPD_MMA_WARPS == 1, "the update epilogue converts all 7 levels of 
 // one k-chunk of a tile with the B planes stacked along N: for A plane pp
 // the pairs (pp, q), q = 0 .. 6 - pp, accumulate into levels pp .. 6, whose
 // TMEM blocks of 64 columns are contiguous, so they are one MMA over B
-// planes 0 .. 6 - pp (N = 64 (7 - pp), split at N = 256): 10 MMAs instead of
+// planes 0 .. 6 - pp (N = 64 (7 - pp), above N = 256 in two equal halves): 10 MMAs instead of
 // 28, and A plane pp is read from shared memory once or twice instead of
 // 7 - pp times.  N >= 128 MMAs run at the tensor pipe's full rate; N = 64
 // ones are bound by shared-memory operand bandwidth.
 __device__ __forceinline__ void upd_issue_chunk(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first) {
 #pragma unroll
   for (int pp = 0; pp < NSLICE; ++pp) {
+    // N = 64 (7 - pp) in one MMA, or, above the 256 limit, in two equal
+    // halves (224 + 224, 192 + 192, 160 + 160): an N = 64 remainder would
+    // be bound by the A operand's shared-memory read rather than the tensor
+    // pipe.  The stacked B rows and the TMEM columns are both contiguous, so
+    // a split at any multiple of 8 rows is one offset in each.
+    const int n = 64 * (NSLICE - pp);
+    const int nh = n <= 256 ? n : n / 2;
 #pragma unroll
-    for (int q0 = 0; q0 < NSLICE - pp; q0 += 4) {
-      const int nq = (NSLICE - pp - q0) < 4 ? (NSLICE - pp - q0) : 4;  // planes in this MMA
-      const uint32_t idesc = (1u << 4) | ((uint32_t)(64 * nq >> 3) << 17) | ((128u >> 4) << 24);
-      mma_f16_desc(tbase + (uint32_t)(pp + q0) * 64, adesc + (uint64_t)(pp * 4096 >> 4),
-                   bdesc + (uint64_t)(q0 * 1024 >> 4), idesc, (first && pp == 0) ? 0u : 1u);
+    for (int off = 0; off < n; off += nh) {
+      const uint32_t idesc = (1u << 4) | ((uint32_t)(nh >> 3) << 17) | ((128u >> 4) << 24);
+      mma_f16_desc(tbase + (uint32_t)(pp * 64 + off), adesc + (uint64_t)(pp * 4096 >> 4),
+                   bdesc + (uint64_t)((off * 16) >> 4), idesc, (first && pp == 0) ? 0u : 1u);
     }
   }
 }
@@ -523,19 +529,20 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint64_t soff = (uint64_t)((st * STAGE) >> 4);
-          // A plane pp against B planes q0 .. stacked along N (at most 256
-          // rows per MMA): levels pp + q0 .. in one instruction
-          constexpr int PL = 256 / N;
+          // A plane pp against B planes 0 .. 6 - pp stacked along N: levels
+          // pp .. 6 in one instruction, or, above N = 256, two equal halves
+          // (as in the trailing update)
 #pragma unroll
-          for (int pp = 0; pp < NSLICE; ++pp)
+          for (int pp = 0; pp < NSLICE; ++pp) {
+            const int n = N * (NSLICE - pp);
+            const int nh = n <= 256 ? n : n / 2;
 #pragma unroll
-            for (int q0 = 0; q0 < NSLICE - pp; q0 += PL) {
-              const int nq = NSLICE - pp - q0 < PL ? NSLICE - pp - q0 : PL;
-              mma_f16_desc(dt + (uint32_t)((pp + q0) * N), adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
-                           bdesc0 + soff + (uint64_t)((q0 * N * 16) >> 4),
-                           (1u << 4) | ((uint32_t)(N * nq >> 3) << 17) | ((128u >> 4) << 24),
+            for (int off = 0; off < n; off += nh)
+              mma_f16_desc(dt + (uint32_t)(pp * N + off), adesc0 + soff + (uint64_t)(pp * 4096 >> 4),
+                           bdesc0 + soff + (uint64_t)((off * 16) >> 4),
+                           (1u << 4) | ((uint32_t)(nh >> 3) << 17) | ((128u >> 4) << 24),
                            (c == 0 && pp == 0) ? 0u : 1u);
-            }
+          }
           mma_commit(&empty[st]);
         }
         if (s_abort) break;
