@@ -12,6 +12,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <atomic>
 #include <mutex>
 #include <new>
 #include <string>
@@ -113,13 +114,18 @@ int compile_spec(const int* kspec, int nkspec, int d, Spec& sp, std::vector<int>
 // each rounded up to 16, fit the 128 digit columns of the panel buffer.  The
 // process-wide build mode (fgpu_set_build_mode; FGPU_BUILD=fp64 at load)
 // can keep the FP64 dot-product build instead.
-int g_build_mode = -1;  // 1: tensor-core build where eligible, 0: FP64 dot-product build
+// Atomic: contexts may be created from several host threads while another
+// thread switches the mode.
+std::atomic<int> g_build_mode{-1};  // 1: tensor-core build where eligible, 0: FP64 dot-product build
 int build_mode() {
-  if (g_build_mode < 0) {
+  int m = g_build_mode.load(std::memory_order_relaxed);
+  if (m < 0) {
     const char* v = getenv("FGPU_BUILD");
-    g_build_mode = (v && (strcmp(v, "fp64") == 0 || strcmp(v, "0") == 0)) ? 0 : 1;
+    const int env = (v && (strcmp(v, "fp64") == 0 || strcmp(v, "0") == 0)) ? 0 : 1;
+    g_build_mode.compare_exchange_strong(m, env, std::memory_order_relaxed);  // m: the value now set
+    if (m < 0) m = env;
   }
-  return g_build_mode;
+  return m;
 }
 
 void plan_tc_build(Spec& sp) {
@@ -205,13 +211,16 @@ struct Workspace {
 // Process-wide default trailing-update mode for contexts created from now on:
 // 1 = tcgen05 split-integer update (128-wide panels), 0 = FP64 mma.sync.
 // The environment variable FGPU_TRAILING=fp64 selects 0 at load time.
-int g_default_mode = -1;
+std::atomic<int> g_default_mode{-1};
 int default_mode() {
-  if (g_default_mode < 0) {
+  int m = g_default_mode.load(std::memory_order_relaxed);
+  if (m < 0) {
     const char* v = getenv("FGPU_TRAILING");
-    g_default_mode = (v && (strcmp(v, "fp64") == 0 || strcmp(v, "0") == 0)) ? 0 : 1;
+    const int env = (v && (strcmp(v, "fp64") == 0 || strcmp(v, "0") == 0)) ? 0 : 1;
+    g_default_mode.compare_exchange_strong(m, env, std::memory_order_relaxed);  // m: the value now set
+    if (m < 0) m = env;
   }
-  return g_default_mode;
+  return m;
 }
 
 // Optional per-launch event pairs for stage timing (captured into the graph).
@@ -908,14 +917,14 @@ int fgpu_nparams(const fgpu_ctx* ctx) { return ctx ? ctx->ntheta : FGPU_EINVAL; 
 int fgpu_set_build_mode(int mode) {
   const int prev = build_mode();
   if (mode != 0 && mode != 1) return fail(FGPU_EINVAL, "build mode must be 0 (fp64) or 1 (tensor cores)");
-  g_build_mode = mode;
+  g_build_mode.store(mode, std::memory_order_relaxed);
   return prev;
 }
 
 int fgpu_set_trailing_update(int mode) {
   const int prev = default_mode();
   if (mode != 0 && mode != 1) return fail(FGPU_EINVAL, "trailing-update mode must be 0 (fp64) or 1 (tcgen05)");
-  g_default_mode = mode;
+  g_default_mode.store(mode, std::memory_order_relaxed);
   return prev;
 }
 
