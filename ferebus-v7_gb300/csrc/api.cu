@@ -1032,6 +1032,7 @@ int make_grad_ws(fgpu_ctx* c, GradWS** out) {
   p.ld = g->ld;
   p.nsteps = g->nsteps;
   p.nrt = g->nrt;
+  p.border_only = c->mode == 1 ? 1 : 0;
   p.nrhs = c->nrhs;
   p.likelihood = c->likelihood;
   p.optimise_noise = c->optimise_noise;
@@ -1072,23 +1073,62 @@ int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, double
     ctx->grad = g;
   }
   GradWS* g = ctx->grad;
+  long long n = 0;
+  Worker* w = nullptr;
+  struct Rel {
+    fgpu_ctx* c;
+    Worker* w;
+    ~Rel() {
+      if (w) release(c, w);
+    }
+  } rel{ctx, nullptr};
   cudaStream_t s = g->stream;
+  if (ctx->mode == 1) {
+    // Tensor-core context: the evaluation itself (factor, log-likelihood,
+    // alpha) is the plain path's graph; its factor L, alpha, the likelihood
+    // epilogue's scalars and status are copied into the adjoint workspace,
+    // whose FP64 sweep then only turns the identity rows into L^-T.  Every
+    // step runs on the worker's stream; the worker is released after the
+    // final synchronisation.
+    int rc = 0;
+    w = acquire(ctx, &rc);
+    if (!w) return rc;
+    rel.w = w;
+    s = w->stream;
+    memcpy(w->h_stage, theta, sizeof(double) * ntheta);
+    CK(cudaMemcpyAsync(w->theta_d, w->h_stage, sizeof(double) * ntheta, cudaMemcpyHostToDevice, s));
+    CK(cudaGraphLaunch(w->graph, s));
+    n += w->graph_kernels;
+    CK(launch_backsolve(w->prob_d, 1, ctx->nsteps, nullptr, s, &n));
+    CK(cudaMemcpy2DAsync(g->ws.K, sizeof(double) * g->ld, w->ws.K, sizeof(double) * ctx->ld,
+                         sizeof(double) * g->Nc, g->Nc, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(g->ws.z, w->ws.z, sizeof(double) * g->Nc, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(g->ws.out, w->ws.out, sizeof(double) * 8, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(g->ws.status, w->ws.status, sizeof(int) * 4, cudaMemcpyDeviceToDevice, s));
+  }
   memcpy(g->h_stage, theta, sizeof(double) * ntheta);
   CK(cudaMemcpyAsync(g->theta_d, g->h_stage, sizeof(double) * ntheta, cudaMemcpyHostToDevice, s));
-  CK(cudaMemsetAsync(g->ws.status, 0, sizeof(int) * 4, s));
-  long long n = 0;
-  CK(launch_build(g->prob_d, 1, g->nsteps, ctx->spec.nplanes, s));
+  if (ctx->mode != 1) {
+    CK(cudaMemsetAsync(g->ws.status, 0, sizeof(int) * 4, s));
+    CK(launch_build(g->prob_d, 1, g->nsteps, ctx->spec.nplanes, s));
+    ++n;
+  }
   CK(launch_identity_border(g->prob_d, g->Nc, s));
-  n += 2;
+  ++n;
   for (int step = 0; step < g->nsteps; ++step) {
-    CK(launch_potf2(g->prob_d, 1, step, s));
+    if (ctx->mode != 1) {
+      CK(launch_potf2(g->prob_d, 1, step, s));
+      ++n;
+    }
     CK(launch_trsm(g->prob_d, 1, step, g->nsteps, s, g->nrt));
     CK(launch_update(g->prob_d, 1, step, g->nsteps, s, g->nrt));
-    n += 3;
+    n += 2;
   }
-  CK(launch_finalize(g->prob_d, 1, s));
-  ++n;
-  CK(launch_backsolve(g->prob_d, 1, g->nsteps, nullptr, s, &n));
+  if (ctx->mode != 1) {
+    CK(launch_finalize(g->prob_d, 1, s));
+    ++n;
+    CK(launch_backsolve(g->prob_d, 1, g->nsteps, nullptr, s, &n));
+  }
   CK(launch_syrk_inv(g->prob_d, g->nsteps, s));
   ++n;
   CK(enqueue_grad_passes(g->prob_d, g->nsteps, ctx->nkparams, ctx->optimise_noise, g->g_d, s, &n));
@@ -1101,6 +1141,8 @@ int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, double
   CK(cudaStreamSynchronize(s));
   t_launches = n;
   if (h_status[2]) return fail(FGPU_ETIMEOUT, "a bounded wait in a kernel gave up");
+  if (h_status[3] && !h_status[1])
+    return fail(FGPU_ECUDA, "panel value outside its row scale bound (split-integer update)");
   *info = h_status[0];
   *ll = (*info == 0) ? h_out[0] : std::nan("");
   for (int k = 0; k < ntheta; ++k) dll[k] = (*info == 0) ? h_g[k] : std::nan("");

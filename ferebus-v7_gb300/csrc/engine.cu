@@ -426,6 +426,7 @@ __global__ void __launch_bounds__(256) k_trsmw(const Prob* __restrict__ probs, i
   // the adjoint's identity rows: zero panel values before their own panel
   // (see k_update), so their solve at earlier panels would leave zeros
   if (r0 / TB > P.nsteps && r0 / TB - (P.nsteps + 1) > col0 / TB) return;
+  if (P.border_only && r0 / TB <= P.nsteps) return;  // the factor is final: identity rows only
   constexpr int LDA = TB + 1;
   __shared__ double L[W * (W + 1)];
   __shared__ double B[W * LDA];
@@ -484,6 +485,7 @@ __global__ void __launch_bounds__(128) k_update(const Prob* __restrict__ probs, 
   // stay exactly zero before panel q (L^-1 is lower triangular), so there
   // is nothing to subtract at earlier steps.
   if (ti > P.nsteps && ti - (P.nsteps + 1) > step) return;
+  if (P.border_only && ti <= P.nsteps) return;  // the factor is final: identity rows only
   if (*(volatile int*)&P.status[1]) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* As = reinterpret_cast<double*>(smem_raw);  // [k][m]

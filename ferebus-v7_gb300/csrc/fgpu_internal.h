@@ -89,6 +89,10 @@ struct Prob {
   // FP64 kernels: number of 64-row tiles when extra border rows follow the
   // right-hand-side tile (the adjoint's identity rows); 0 = nsteps + 1
   int nrt;
+  // adjoint on a tensor-core context: K already holds the final factor L
+  // (from the tensor-core evaluation), so the FP64 sweep works only on the
+  // identity rows below the right-hand-side tile
+  int border_only;
   double* kinv;                   // adjoint: K^-1 (Nc x Nc, lower)
   double* gpart;                  // adjoint: per-CTA partial sums
   // tensor-core build

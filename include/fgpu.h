@@ -116,10 +116,12 @@ int fgpu_loglik_batch(fgpu_ctx* const* ctxs, int nprob, const double* const* the
 /* Log-likelihood and its gradient d logL / d theta (including the noise
  * parameter when optimise_noise is set) by the FP64 adjoint
  * 1/2 tr((alpha alpha^T / s - K^-1) dK/dtheta), s = 1 (marginal) or sigma^2
- * (concentrated).  The reference has no analytic likelihood gradient
- * (negative_log_likelihood, gpr.f90:258-289, accepts but ignores
- * gradient=.true.); this is the optional gradient polish.  dll_dtheta has
- * fgpu_nparams(ctx) entries. */
+ * (concentrated).  The factor is the evaluation's own (on a tensor-core
+ * context the same factor, log-likelihood and alpha as fgpu_loglik), K^-1
+ * comes from it in FP64, and dK is recomputed tile by tile.  The reference
+ * has no analytic likelihood gradient (negative_log_likelihood,
+ * gpr.f90:258-289, accepts but ignores gradient=.true.); this is the
+ * optional gradient polish.  dll_dtheta has fgpu_nparams(ctx) entries. */
 int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll,
               double* dll_dtheta, int* info);
 
