@@ -494,8 +494,9 @@ def main():
         eng.loglik(th_host[args.warmup][k % S])
     plain_v = args.plain / (time.perf_counter() - t0)
 
-    # the FP64 adjoint (gradient polish) at the same shape, one particle:
-    # algorithmic FP64 work N^3 (Cholesky N^3/3, triangular inverse N^3/3,
+    # the adjoint (gradient polish) at the same shape, one particle: the
+    # factor, likelihood and alpha from the tensor-core evaluation (the plain
+    # path's graph), then FP64 work 2 N^3 / 3 (triangular inverse N^3/3,
     # K^-1 = L^-T L^-1 N^3/3) + the fused dK pass (~10 flops per entry and dim)
     eng.grad(th_host[0][0])
     torch.cuda.synchronize()
@@ -503,7 +504,7 @@ def main():
     for k in range(2):
         eng.grad(th_host[args.warmup][k])
     grad_s = (time.perf_counter() - t0) / 2
-    grad_flops = float(p.N) ** 3 + 10.0 * p.N * (p.N + 1) / 2 * p.d
+    grad_flops = 2.0 * float(p.N) ** 3 / 3.0 + 10.0 * p.N * (p.N + 1) / 2 * p.d
 
     # per-stage breakdown (diagnostic): one more, untimed replay with event
     # nodes around every launch
@@ -600,7 +601,8 @@ def main():
             "grad": {"ms": grad_s * 1e3, "fp64_flops": grad_flops,
                      "fp64_tflops": grad_flops / grad_s / 1e12, "fp64_peak_tflops": fp64_peak,
                      "frac": grad_flops / grad_s / 1e12 / fp64_peak,
-                     "what": "fgpu_grad (d logL / d theta, FP64 adjoint), one particle, host wall clock"},
+                     "what": "fgpu_grad (d logL / d theta), one particle, host wall clock: the tensor-core "
+                             "evaluation's factor, then K^-1 and the dK pass in FP64 (fp64_flops: that FP64 part)"},
             "batched_over_plain": value / ws / plain_v if plain_v else None,
             "shapes": shapes,
             "cholesky_failure_rate": fail_rate}
