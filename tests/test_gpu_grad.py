@@ -1,9 +1,9 @@
-"""The FP64 adjoint (fgpu_grad) against the oracle's analytic FP64 gradient
-and central finite differences.
+"""The adjoint (fgpu_grad) against the oracle's analytic FP64 gradient and
+central finite differences.
 
-Target (the benchmark spec): d logL / d theta within 1e-6 relative of the
-FP64 oracle.  Per component: |g - g_ref| <= 1e-6 |g_ref| + 1e-9 max|g_ref|
-(the absolute slack covers components that cancel to ~0).
+Target: d logL / d theta within 1e-6 relative of the FP64 oracle.  Per
+component: |g - g_ref| <= 1e-6 |g_ref| + 1e-9 max|g_ref| (the absolute slack
+covers components that cancel to ~0).
 """
 import numpy as np
 import pytest
