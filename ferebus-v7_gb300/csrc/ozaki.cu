@@ -623,29 +623,30 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) kn[jj] = more ? kcol[(size_t)((g + 1) * 8 + jj) * ld] : 0.0;
         asm volatile("tcgen05.wait::ld.sync.aligned;");
-        // the exact level sums from their magic-added bits (see level_bits),
-        // in place: a sum outside [-2^22, 2^22) (possible only for N = 64,
-        // levels >= 3) sends the warp back to the level sums, still in TMEM,
-        // and F2I
-        uint32_t band = 0xFFFFFFFFu, bor = 0u;
-#pragma unroll
-        for (int l = 0; l < NSLICE; ++l)
-#pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            v[l][jj] = level_bits(v[l][jj]);
-            band &= v[l][jj];
-            bor |= v[l][jj];
-          }
-        const bool slow = NQ > 1 && __any_sync(0xffffffffu, !level_bits_valid(band, bor));
-        if (slow) {
+        // the exact level sums from their magic-added bits (see level_bits)
+        // when every sum of the warp's group lies in (-2^22, 2^22): always
+        // for N = 32 (7 x 32 x 2^14 < 2^22); for N = 64 checked on the raw
+        // sums, the warp converting with F2I otherwise -- so no second TMEM
+        // read is needed and the buffer is released as soon as the tile's
+        // last group is in registers, before that group converts
+        bool slow = false;
+        if constexpr (NQ > 1) {
+          float mx = 0.0f;
 #pragma unroll
           for (int l = 0; l < NSLICE; ++l)
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                         : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
-                           "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
-                         : "r"(tbase + (uint32_t)buf * 256 + ((uint32_t)(lq * 32) << 16) +
-                               (uint32_t)(l * N + hf * NH + g * 8)));
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) mx = fmaxf(mx, fabsf(__uint_as_float(v[l][jj])));
+          slow = !__all_sync(0xffffffffu, mx < 4194304.0f);
+        }
+        if (g == NH / 8 - 1) {
+          asm volatile("tcgen05.fence::before_thread_sync;");
+          mbar_arrive(&tempty[buf]);  // this buffer is free for the tile after next (or the next, N = 64)
+        }
+        if (!slow) {
+#pragma unroll
+          for (int l = 0; l < NSLICE; ++l)
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) v[l][jj] = level_bits(v[l][jj]);
         }
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) {
@@ -669,8 +670,6 @@ __global__ void __launch_bounds__(CPL_THREADS, 1)
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) kv[jj] = kn[jj];
       }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      mbar_arrive(&tempty[buf]);
       if (ti == s) {
         // the problem's own row tile holds quarter dq's diagonal block: factor it
         bar_sync_n(1, CPL_EPI);  // every coupled entry of the tile written and visible
