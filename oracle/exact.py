@@ -1,4 +1,4 @@
-"""Extended-precision log-likelihood: the "exact" value FP64 codes are judged by.
+"""Extended-precision log-likelihood: the "exact" value FP64 codes are measured against.
 
 TEST INFRASTRUCTURE ONLY (like the rest of ``oracle/``): nothing in the
 product imports it; the tests and the fixture generator use it as a checker.
@@ -8,7 +8,7 @@ Why it exists.  With the reference's default nugget of 1e-10
 is nearly singular (cond(K) ~ 1e10-1e12), and two standard FP64 LAPACKs
 evaluating the same formulas on the same K disagree by up to ~1e-5 of logL
 (OpenBLAS vs MKL on the water-like set).  Neither is "the" answer, so an FP64
-code cannot be judged by its distance to one of them.  This module evaluates
+code cannot be measured by its distance to one of them.  This module evaluates
 the reference's formulas with a 64-bit significand instead of 53 bits
 (numpy ``longdouble``: x87 80-bit extended on x86-64, IEEE binary128 on
 aarch64), so its result is ~2000 times (x86-64) or more closer to the exact
