@@ -185,14 +185,11 @@ __device__ __forceinline__ long long levels_to_w64(const int S[7]) {
 
 // Exact integer level sums without the conversion unit.  For an
 // integer-valued float x with -2^22 <= x < 2^22, x + 1.5 2^23 is exact and
-// its bits b = 0x4B000000 + (x + 2^22) agree with 0x4B000000 in bits 23..31;
-// any other x with |x| <= 2^24 changes those bits.  A group of such bits is
-// valid when the AND and the OR of the group both still agree there.
+// its bits are b = 0x4B000000 + (x + 2^22).  Callers establish the range
+// first: by a bound on the contraction, or by checking the raw sums of a
+// warp's group (|x| < 2^22) and converting with F2I otherwise.
 __device__ __forceinline__ uint32_t level_bits(uint32_t v) {
   return __float_as_uint(__uint_as_float(v) + 12582912.0f);
-}
-__device__ __forceinline__ bool level_bits_valid(uint32_t band, uint32_t bor) {
-  return (((band ^ 0x4B000000u) | (bor ^ 0x4B000000u)) >> 23) == 0u;
 }
 
 // W = sum_l x_l 256^(6 - l) from the valid bits b_l of column jj's 7 level
