@@ -1167,6 +1167,10 @@ int fgpu_plan_create(fgpu_plan** out, fgpu_ctx* const* ctxs, int nprob, int ldth
     p->ctxs.push_back(ctxs[i]);
   }
   if (ldtheta < maxth) return fail(FGPU_EINVAL, "ldtheta=%d < max nparams %d", ldtheta, maxth);
+  // the couplings' row-tile order packs (problem << 16 | row tile) into a
+  // non-negative int (a negative entry ends a CTA's work)
+  if (ctxs[0]->mode == 1 && nprob > 32767)
+    return fail(FGPU_EINVAL, "a tensor-core plan holds at most 32767 problems (%d given)", nprob);
   p->ldtheta = ldtheta;
   p->mode = ctxs[0]->mode;
   CK(cudaSetDevice(p->device));

@@ -128,6 +128,7 @@ int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll,
 /* Device-resident batch plan (inputs and outputs stay in HBM).  theta_dev is
  * nprob x ldtheta doubles on the device; ll_dev / info_dev are device arrays of
  * nprob entries.  stream is a cudaStream_t (NULL = the plan's own stream).
+ * A plan holds at most 65535 problems, 32767 on tensor-core contexts.
  * Used by the throughput benchmark and by hosts that keep the swarm on the GPU.
  * A plan whose problems' workspaces exceed the device-memory budget (the
  * free memory less a reserve, or FGPU_PLAN_MEM_BUDGET_MB) runs them in waves

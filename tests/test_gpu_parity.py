@@ -174,6 +174,29 @@ def test_invalid_theta_is_an_error_not_a_fault(lib):
     assert e.loglik(th)[1] == 0  # context still usable
 
 
+def test_plan_size_limits_are_errors(lib):
+    """A plan takes at most 65535 problems (one grid row each), a tensor-core
+    plan at most 32767 (its couplings' row-tile order packs problem << 16 |
+    row tile into a non-negative int); larger ones are argument errors
+    raised before any device work."""
+    from fgpu import Engine, Plan
+    from fgpu._lib import FgpuError
+    from fgpu.gpr import set_trailing_update
+    X, y, mu, ks, th = _random_problem(40, 3, 0, seed=3)
+    engines = {}
+    for mode in ("tcgen05", "fp64"):
+        prev = set_trailing_update(mode)
+        try:
+            engines[mode] = Engine(X, y, mu, ks, 0, 1e-6, False)
+        finally:
+            set_trailing_update(prev)
+    for mode, n in (("tcgen05", 32768), ("tcgen05", 65536), ("fp64", 65536)):
+        with pytest.raises(FgpuError) as err:
+            Plan([engines[mode]] * n)
+        assert err.value.code == -1, (mode, n)  # FGPU_EINVAL
+    assert engines["tcgen05"].loglik(th)[1] == 0  # contexts still usable
+
+
 def test_full_size_glycine_like_config(lib):
     """N=4000, d=24 (the benchmark workload): batch of particles == plain calls,
     and one particle against the oracle."""
