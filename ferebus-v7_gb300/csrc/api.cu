@@ -797,6 +797,26 @@ size_t plan_cache_limit() {
   return (size_t)(n > 0 ? n : 1);
 }
 
+// Frees an adjoint workspace, complete or partly built (unset members are null).
+void free_grad_ws(GradWS* g) {
+  if (!g) return;
+  for (void* q : {(void*)g->ws.K, (void*)g->ws.logdet_part, (void*)g->ws.status, (void*)g->ws.out,
+                  (void*)g->ws.z, (void*)g->kinv, (void*)g->gpart, (void*)g->theta_d, (void*)g->g_d,
+                  (void*)g->prob_d})
+    cudaFree(q);
+  if (g->h_stage) cudaFreeHost(g->h_stage);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+}
+struct GradWSDeleter {
+  void operator()(GradWS* g) const { free_grad_ws(g); }
+};
+// A context that fgpu_create could not finish is destroyed with everything
+// it had allocated.
+struct CtxDeleter {
+  void operator()(fgpu_ctx* c) const { fgpu_destroy(c); }
+};
+
 }  // namespace
 
 extern "C" {
@@ -817,7 +837,7 @@ int fgpu_create(fgpu_ctx** out, int N, int d, const double* X, const double* y, 
   if (likelihood == FGPU_MARGINAL && !mu) return fail(FGPU_EINVAL, "marginal likelihood needs mu");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(FGPU_ENODEV, "no CUDA device");
-  std::unique_ptr<fgpu_ctx> c(new (std::nothrow) fgpu_ctx());
+  std::unique_ptr<fgpu_ctx, CtxDeleter> c(new (std::nothrow) fgpu_ctx());
   if (!c) return fail(FGPU_ENOMEM, "context allocation");
   CK(cudaGetDevice(&c->device));
   std::vector<int> plane_dim, plane_kind;
@@ -948,16 +968,7 @@ void fgpu_destroy(fgpu_ctx* ctx) {
   cudaGetDevice(&prev);
   cudaSetDevice(ctx->device);
   for (Worker* w : ctx->workers) free_worker(w);
-  if (ctx->grad) {
-    GradWS* g = ctx->grad;
-    for (void* q : {(void*)g->ws.K, (void*)g->ws.logdet_part, (void*)g->ws.status, (void*)g->ws.out,
-                    (void*)g->ws.z, (void*)g->kinv, (void*)g->gpart, (void*)g->theta_d, (void*)g->g_d,
-                    (void*)g->prob_d})
-      cudaFree(q);
-    if (g->h_stage) cudaFreeHost(g->h_stage);
-    if (g->stream) cudaStreamDestroy(g->stream);
-    delete g;
-  }
+  free_grad_ws(ctx->grad);
   cudaFree(ctx->planes64_d);
   cudaFree(ctx->planes_d);
   cudaFree(ctx->plane_max_d);
@@ -1006,7 +1017,7 @@ int fgpu_loglik(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll, int*
 
 namespace {
 int make_grad_ws(fgpu_ctx* c, GradWS** out) {
-  std::unique_ptr<GradWS> g(new (std::nothrow) GradWS());
+  std::unique_ptr<GradWS, GradWSDeleter> g(new (std::nothrow) GradWS());  // freed whole on failure
   if (!g) return fail(FGPU_ENOMEM, "adjoint workspace");
   g->Nc = round_up(c->N, TB);
   g->nsteps = g->Nc / TB;
