@@ -129,6 +129,10 @@ int fgpu_grad(fgpu_ctx* ctx, const double* theta, int ntheta, double* ll,
  * nprob x ldtheta doubles on the device; ll_dev / info_dev are device arrays of
  * nprob entries.  stream is a cudaStream_t (NULL = the plan's own stream).
  * A plan holds at most 65535 problems, 32767 on tensor-core contexts.
+ * A plan owns one set of workspaces: its runs must not overlap on the GPU
+ * (fgpu_plan_run_device calls on different streams, or one on a stream other
+ * than the plan's followed by fgpu_plan_run, race unless the caller orders
+ * them); fgpu_plan_run returns after its run has finished.
  * Used by the throughput benchmark and by hosts that keep the swarm on the GPU.
  * A plan whose problems' workspaces exceed the device-memory budget (the
  * free memory less a reserve, or FGPU_PLAN_MEM_BUDGET_MB) runs them in waves
