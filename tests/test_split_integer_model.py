@@ -8,7 +8,7 @@ meets the parity tolerance (conftest.parity_tol, against the
 extended-precision value); with fewer
 levels some do not, which shows that the test can fail and that 7 is the
 smallest level count the fixtures accept (measured: 6 levels miss the
-ammonia set by ~2400x its tolerance, 5 levels by ~4e4x).  A second model
+ammonia set by ~2600x its tolerance, 5 levels by ~4e4x).  A second model
 (`factor_quarters`) also restates the engine's work inside a panel: the
 32-column quarters with digit-plane couplings between and within them.
 """
