@@ -34,6 +34,47 @@ def test_version_string(lib):
     assert b"sm_103a" in lib.fgpu_version()
 
 
+_C_HOST = r"""
+#include "fgpu.h"
+#include <stdio.h>
+#include <string.h>
+int main(void) {
+  long long bytes[4] = {40, 30, 20, 10};
+  int wave_of[4], nwaves = 0;
+  if (strstr(fgpu_version(), "sm_103a") == NULL) return 2;
+  if (fgpu_plan_partition(bytes, 4, 50, wave_of, &nwaves) != 0) return 3;
+  printf("%d %d %d %d %d\n", nwaves, wave_of[0], wave_of[1], wave_of[2], wave_of[3]);
+  if (fgpu_loglik(NULL, NULL, 0, NULL, NULL, NULL) != FGPU_EINVAL) return 4;
+  printf("%s\n", fgpu_last_error());
+  return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("compiler", [["gcc", "-std=c99", "-x", "c"], ["g++", "-std=c++17", "-x", "c++"]])
+def test_header_serves_a_c_host(lib, tmp_path, compiler):
+    """A plain C (and a C++) program includes include/fgpu.h with every
+    warning an error, links libfgpu.so and calls host-only entry points:
+    the wave partition (40, 30, 20, 10 bytes under a budget of 50: waves
+    0 | 1 1 | 2) and an argument error."""
+    import shutil
+    from fgpu.build import LIB_DIR
+    if shutil.which(compiler[0]) is None:
+        pytest.skip(f"{compiler[0]} not installed")
+    src = tmp_path / "host.c"
+    src.write_text(_C_HOST)
+    exe = tmp_path / "host"
+    cmd = [*compiler, "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"), str(src),
+           "-x", "none", "-L", LIB_DIR, "-lfgpu", f"-Wl,-rpath,{LIB_DIR}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    lines = r.stdout.splitlines()
+    assert lines[0] == "3 0 1 1 2"
+    assert lines[1] == "NULL argument"
+
+
 @pytest.mark.skipif(gpu_available(), reason="checks the no-device error path")
 def test_create_without_device_fails_cleanly(lib):
     from fgpu import _lib
