@@ -108,7 +108,11 @@ class TuneCache:
     def put(self, key, choice, ms):
         self.data[key] = {"choice": choice.name, "ms": ms}
         os.makedirs(os.path.dirname(os.path.abspath(self.path)), exist_ok=True)
-        tmp = self.path + ".tmp"
+        # a temporary file of this process's own, renamed over the cache in
+        # one step: ranks of one job that tune at the same time never share
+        # the temporary (one's rename would leave the other nothing to
+        # rename) and a reader sees one whole file or the other
+        tmp = f"{self.path}.{os.getpid()}.tmp"
         with open(tmp, "w") as f:
             json.dump(self.data, f, indent=1, sort_keys=True)
         os.replace(tmp, self.path)

@@ -1,6 +1,12 @@
 """The autotuner's host logic with a fake timer (no GPU): it picks the
 fastest candidate per shape, caches the choice by shape key, samples the
-largest problems, and never picks a candidate that failed to run."""
+largest problems, never picks a candidate that failed to run, and saves its
+cache safely from several processes at once."""
+import json
+import multiprocessing as mp
+import os
+import sys
+
 import numpy as np
 import pytest
 
@@ -72,3 +78,32 @@ def test_shape_key_buckets():
 def test_config_names_round_trip():
     for c in A.CANDIDATES:
         assert A.Config.from_name(c.name) == c
+
+
+
+PKG = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "ferebus-v7_gb300")
+
+
+def _put_many(path, rank, n):
+    sys.path.insert(0, PKG)
+    from fgpu import autotune as A2
+    for k in range(n):
+        A2.TuneCache(path).put(f"rank{rank}-{k}", A2.Config.from_name("tcgen05/tc"), {"tcgen05/tc": 1.0})
+
+
+def test_ranks_saving_the_cache_at_once(tmp_path):
+    """Several processes (the ranks of one job, tuning on a fresh machine at
+    the same time) save the cache concurrently: none fails, and the file is
+    always one whole JSON document."""
+    path = str(tmp_path / "tune.json")
+    ctx = mp.get_context("spawn")
+    procs = [ctx.Process(target=_put_many, args=(path, r, 40)) for r in range(4)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+    assert [p.exitcode for p in procs] == [0, 0, 0, 0]
+    with open(path) as f:
+        data = json.load(f)
+    assert data and all(v["choice"] == "tcgen05/tc" for v in data.values())
+    assert not [n for n in os.listdir(tmp_path) if n.endswith(".tmp")]
