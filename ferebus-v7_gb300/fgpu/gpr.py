@@ -19,7 +19,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from .kernel_spec import build_kspec, nparams as spec_nparams
+from .kernel_spec import CONSTANT, build_kspec, parse_kspec, nparams as spec_nparams
 
 MARGINAL, CONCENTRATED = 0, 1
 LIKELIHOODS = {"marginal": MARGINAL, "concentrated": CONCENTRATED}
@@ -262,8 +262,21 @@ class GaussianProcessRegressor:
         self.engine = engine or Engine(X, self.y, self.cached_mean, self.kspec, self.likelihood, noise,
                                        optimise_noise)
         self._search = (float(search_min), float(search_max))
+        # a number in the expression is a constant kernel whose parameter is
+        # its value, starting at that number (visit_numop,
+        # src/interpreter/ast.f90:257-271); the other parameters start at 0
+        # here (the swarm sets every parameter before the first evaluation)
         self.params = np.zeros(self.nparams())
-        self.params[:len(consts)] = 0.0
+        off, k = 0, 0
+        for node in parse_kspec(self.kspec):
+            if node[0] != "leaf":
+                continue
+            if node[1] == CONSTANT:
+                self.params[off] = float(consts[k])
+                k += 1
+                off += 1
+            else:
+                off += len(node[2])
 
     def nparams(self):
         return spec_nparams(self.kspec) + (1 if self.optimise_nugget else 0)

@@ -35,6 +35,24 @@ def test_numbers_become_constant_kernels():
     assert nparams(ks) == 4
 
 
+@pytest.mark.parametrize("expr,where", [("k1+0.5", 3), ("2.5*k1+0.5", 0), ("k2+(1.5*k1)", 1)])
+def test_constant_parameters_start_at_their_value(expr, where):
+    """A number's constant kernel starts with its value as its parameter, at
+    its own place in the parameter vector (leaf order); the engine is not
+    touched (a stand-in is passed)."""
+    import numpy as np
+    from fgpu.gpr import GaussianProcessRegressor
+    X = np.random.default_rng(0).normal(size=(5, 3))
+    gp = GaussianProcessRegressor(X, X[:, 0], expr, KS, engine=object())
+    ks, consts = build_kspec(expr, KS, 3)
+    p = gp.get_params()
+    assert p.size == nparams(ks)
+    assert p[where] == consts[0]
+    if len(consts) > 1:
+        assert p[-1] == consts[1]
+    assert np.count_nonzero(p) == len(consts)
+
+
 def test_leaf_order_is_parameter_order():
     ks, _ = build_kspec("k4*(k2+k1)", KS, 3)
     leaves = [n for n in parse_kspec(ks) if n[0] == "leaf"]
