@@ -389,8 +389,10 @@ __global__ void __launch_bounds__(UPD_THREADS, 1)
 // NQ = 1, one of 7 x 64 for NQ = 2), warps 0-15 drain the level sums (warps
 // w, w + 4, w + 8, w + 12 share TMEM lanes 32 (w % 4) and take a quarter of
 // the columns each, in groups of 8 with the next group's K entries in
-// flight; four warps per SMSP hide the integer conversion's latency) and
-// subtract the exactly converted sums from K; warp 18 applies the same
+// flight; four warps per SMSP hide the integer conversion's latency; a
+// warp frees its share of the buffer once the tile's last group is in
+// registers, before that group converts) and subtract the exactly
+// converted sums from K; warp 18 applies the same
 // coupling to the right-hand-side rows in FP64.  Once the epilogue warps have coupled a
 // problem's own 128-row tile (barrier 1), warps 0-3 factor quarter dq's
 // 32 x 32 diagonal block right there (barrier 2).
