@@ -12,7 +12,9 @@ periodic_kernel.f90:111-118, 181-206, kernel_module.f90:309-375), the nugget
 (likelihood.f90:161-253) measures it on a clustered, water-like set of 40
 points: the extended-precision error must stay below 1 % of the FP64 error
 scale (measured: 4e-5 to 2e-4 of it), and the oracle's own FP64 value must
-meet the bar the engine is held to.
+meet the bar the engine is held to.  The stored extended-precision values of
+the two fixtures cut from the reference's WATER example (59 points) are
+checked the same way.
 """
 import numpy as np
 import pytest
@@ -23,19 +25,51 @@ from oracle import gpr_oracle as O
 mp = pytest.importorskip("mpmath")
 
 
-def _loglik_mp(X, y, mu, th, noise, likelihood):
-    """logL of rbf(dims 0, 1) x periodic(dim 2), in mpmath."""
+def _loglik_mp(kspec, th, X, y, mu, noise, likelihood):
+    """logL of a kernel spec of rbf / periodic / constant leaves and sums /
+    products, in mpmath (parameters in leaf order)."""
     with mp.workdps(40):
         n = X.shape[0]
-        inv_rbf = [mp.exp(mp.mpf(float(t))) for t in th[:2]]   # the rbf transform e^theta
-        inv_per = (1 / mp.exp(mp.mpf(float(th[2])))) ** 2      # the periodic transform (1/e^theta)^2
         Xm = [[mp.mpf(float(v)) for v in row] for row in X]
+        leaves, p = [], 0
+        for node in O.parse_kspec(kspec):
+            if node[0] == "leaf":
+                _, op, dims = node
+                t = [mp.mpf(float(v)) for v in th[p:p + O.leaf_nparams(op, dims)]]
+                p += len(t)
+                if op == O.RBF:
+                    prm = [mp.exp(v) for v in t]                   # e^theta
+                elif op == O.PERIODIC:
+                    prm = [(1 / mp.exp(v)) ** 2 for v in t]        # (1/e^theta)^2
+                elif op == O.CONSTANT:
+                    prm = t
+                else:
+                    raise ValueError(op)
+                leaves.append((op, dims, prm))
+
+        def k(i, j):
+            stack, q = [], 0
+            for node in O.parse_kspec(kspec):
+                if node[0] == "leaf":
+                    op, dims, prm = leaves[q]
+                    q += 1
+                    if op == O.RBF:
+                        a = mp.fsum((Xm[i][dd] - Xm[j][dd]) ** 2 * w for dd, w in zip(dims, prm))
+                        stack.append(mp.exp(-a / 2))
+                    elif op == O.PERIODIC:
+                        a = mp.fsum(mp.sin(abs(Xm[i][dd] - Xm[j][dd]) / 2) ** 2 * w for dd, w in zip(dims, prm))
+                        stack.append(mp.exp(-2 * a))
+                    else:
+                        stack.append(prm[0])
+                else:
+                    b, a = stack.pop(), stack.pop()
+                    stack.append(a + b if node[1] == O.SUM else a * b)
+            return stack[0]
+
         K = mp.matrix(n, n)
         for i in range(n):
             for j in range(i + 1):
-                a = sum((Xm[i][k] - Xm[j][k]) ** 2 * inv_rbf[k] for k in range(2))
-                s = mp.sin(abs(Xm[i][2] - Xm[j][2]) / 2)
-                v = mp.exp(-a / 2) * mp.exp(-2 * s * s * inv_per)
+                v = k(i, j)
                 if i == j:
                     v += mp.mpf(float(noise))
                 K[i, j] = K[j, i] = v
@@ -67,7 +101,7 @@ def test_extended_precision_error_is_far_below_the_fp64_error(likelihood, theta)
     ks = [O.RBF, 2, 1, 2, O.PERIODIC, 1, 3, O.PROD]
     th = np.array(theta)
     ex = E.loglik_ld(ks, th, X, y, mu, likelihood, noise, False, want=True)
-    ref = _loglik_mp(X, y, mu, th, noise, likelihood)
+    ref = _loglik_mp(ks, th, X, y, mu, noise, likelihood)
     err_ld = abs(float(ex["ll_ld"] - np.longdouble(mp.nstr(ref, 30))))
     err64, _ = E.fp64_error_scale(ks, th, X, y, mu, likelihood, noise, False, ex["ll"])
     assert err64 > 1e-9 * abs(float(ref))  # ill-conditioned: no FP64 code meets 1e-9 here
@@ -75,3 +109,19 @@ def test_extended_precision_error_is_far_below_the_fp64_error(likelihood, theta)
     ll64, info = O.loglik(ks, th, X, y, mu, likelihood, noise, False)
     assert info == 0
     assert abs(ll64 - float(ref)) <= 2.0 * err64  # OpenBLAS's value meets the engine's bar
+
+
+@pytest.mark.parametrize("name", ["water_H2_rbf_plus_per", "water_O1_rbf_x_per"])
+def test_stored_exact_values_of_the_water_fixtures(name):
+    """The fixtures cut from the reference's WATER example (59 points, nugget
+    1e-10): their stored extended-precision values are within 1 % of their
+    FP64 error scale of the 40-digit value."""
+    from conftest import load_case
+    c = load_case(name)
+    ks = [int(v) for v in c["kspec"]]
+    for k, th in enumerate(c["thetas"]):
+        if c["info"][k] != 0:
+            continue
+        ref = _loglik_mp(ks, th, c["X"], c["y"], c["mu"], float(c["noise"]), int(c["likelihood"]))
+        err = abs(float(c["ll_exact"][k]) - float(ref))
+        assert err <= 0.01 * float(c["fp64_err"][k]), (k, err, float(c["fp64_err"][k]))
