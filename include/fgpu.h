@@ -158,6 +158,11 @@ int fgpu_plan_waves(const fgpu_plan* plan, int* nwaves, long long* arena_bytes);
  * problem i's wave).  Touches no device; for checking the partition rule. */
 int fgpu_plan_partition(const long long* bytes, int n, long long budget, int* wave_of, int* nwaves);
 
+/* Frees a context, its workers, its adjoint workspace and the plans
+ * fgpu_loglik_batch cached for it.  Call it only after every call that uses
+ * the context has returned and every plan built over it (fgpu_plan_create)
+ * has been destroyed or will not run again: those plans read the context's
+ * training data on the device. */
 void fgpu_destroy(fgpu_ctx* ctx);
 
 /* One evaluation that allocates no device memory.  No counterpart in the
