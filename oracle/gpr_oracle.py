@@ -34,10 +34,12 @@ scipy's bundled OpenBLAS through ``scipy.linalg.lapack``.
 PARITY UNPINNED: the reference ships no tests, golden vectors or known-answer
 tests, and it cannot be built in this environment (pure Fortran, no Fortran
 compiler, its toml-f dependency is an empty submodule).  This restatement is
-cross-checked only against itself: the distance-tensor path against the
-pairwise ``k`` path of the same kernels, OpenBLAS against an independent
-LAPACK (torch/MKL) and a pure-Python Cholesky, and the analytic gradient
-against central finite differences.
+cross-checked only against restatements: the distance-tensor path against
+the pairwise ``k`` path of the same kernels, OpenBLAS against an independent
+LAPACK (torch/MKL) and a pure-Python Cholesky, the analytic gradient against
+central finite differences, the C restatement (ref_cpu.c) against this
+module's fixtures, and the extended-precision evaluation (exact.py) that
+parity is measured against, against 40-digit mpmath arithmetic.
 """
 from __future__ import annotations
 
